@@ -1,0 +1,1221 @@
+// api.cu — the C ABI (include/necstar_gpu.h): state handles, validation in
+// the reference's error order, gate lowering, and the host drivers of
+// projection, measurement and sampling.  All heavy work runs in the kernels
+// of kernels_terms.cu and kernels_pairs.cu; nothing here falls back to a CPU
+// implementation of the pair sums or of the CH-form updates of compiled
+// terms (the |T⟩^{⊗t} expansion, a per-t constant input, is built on the
+// host once per process and cached).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/necstar_gpu.h"
+#include "chform_host.hpp"
+#include "device_state.hpp"
+#include "host_rng.hpp"
+
+using namespace nsg;
+
+// ---------------------------------------------------------------------------
+// Errors
+namespace {
+
+thread_local std::string g_msg;
+thread_local int64_t g_args[3] = {-1, -1, -1};
+
+struct ApiError {
+    nsg_status code;
+};
+
+[[noreturn]] void raise(nsg_status code, int64_t a, int64_t b, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_msg = buf;
+    g_args[0] = a;
+    g_args[1] = b;
+    g_args[2] = -1;
+    throw ApiError{code};
+}
+
+const char* gate_name(uint32_t op) {  // QuantumGate::name (crates/necstar/src/circuit/gates.rs:209-226)
+    static const char* names[] = {"H", "X", "Y", "Z", "S", "Sdg", "SqrtX", "SqrtXdg",
+                                  "CX", "CZ", "Swap", "T", "Tdg", "CCX"};
+    return op < 14 ? names[op] : "?";
+}
+
+// Messages follow the thiserror texts of crates/necstar/src/error/mod.rs:10-91
+// and crates/stabilizer-ch-form-rust/src/error/mod.rs:7-67.
+[[noreturn]] void err_oob(int64_t q, int64_t n) {
+    raise(NSG_ERR_QUBIT_INDEX_OUT_OF_BOUNDS, q, n, "Qubit index %lld is out of bounds for %lld qubits.",
+          (long long)q, (long long)n);
+}
+[[noreturn]] void err_dup_gate(int64_t q) {
+    raise(NSG_ERR_DUPLICATE_QUBIT_INDICES, q, -1,
+          "Two-qubit gate requires two different qubit indices, but got the same: %lld.", (long long)q);
+}
+[[noreturn]] void err_impossible(int64_t q, bool desired) {
+    raise(NSG_ERR_IMPOSSIBLE_PROJECTION, q, desired ? 1 : 0,
+          "Impossible projection on qubit %lld: cannot project determined state |%d> onto |%d>.", (long long)q,
+          desired ? 0 : 1, desired ? 1 : 0);
+}
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) {
+        raise(NSG_ERR_CUDA, (int64_t)e, -1, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+    }
+}
+#define CK(x) cuda_check((x), #x)
+
+// ---------------------------------------------------------------------------
+// Device buffers
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t st = nullptr;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept { *this = std::move(o); }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            p = o.p;
+            n = o.n;
+            st = o.st;
+            o.p = nullptr;
+            o.n = 0;
+        }
+        return *this;
+    }
+    void alloc(size_t count, cudaStream_t s) {
+        release();
+        st = s;
+        n = count;
+        if (count) {
+            cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), s);
+            if (e == cudaErrorMemoryAllocation)
+                raise(NSG_ERR_OUT_OF_MEMORY, (int64_t)(count * sizeof(T)), -1, "device allocation of %zu bytes failed",
+                      count * sizeof(T));
+            cuda_check(e, "cudaMallocAsync");
+        }
+    }
+    void rehome(cudaStream_t s) { st = s; }
+    void release() {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+        n = 0;
+    }
+    ~DBuf() { release(); }
+};
+
+struct TermStore {
+    int n = 0, W = 1, R = 64;
+    int64_t chi = 0, cap = 0;
+    DBuf<uint64_t> G, F, M, V, S, GL, GH;
+    DBuf<uint8_t> phase, ck;
+    DBuf<int32_t> cr;
+
+    void alloc(int n_, int64_t cap_, cudaStream_t st) {
+        n = n_;
+        W = n <= 64 ? 1 : 2;
+        R = 64 * W;
+        cap = std::max<int64_t>(cap_, 1);
+        size_t rows = (size_t)cap * R * W, vec = (size_t)cap * W;
+        G.alloc(rows, st);
+        F.alloc(rows, st);
+        M.alloc(rows, st);
+        V.alloc(vec, st);
+        S.alloc(vec, st);
+        GL.alloc(vec, st);
+        GH.alloc(vec, st);
+        phase.alloc(cap, st);
+        ck.alloc(cap, st);
+        cr.alloc(cap, st);
+    }
+    void rehome(cudaStream_t st) {
+        G.rehome(st); F.rehome(st); M.rehome(st); V.rehome(st); S.rehome(st);
+        GL.rehome(st); GH.rehome(st); phase.rehome(st); ck.rehome(st); cr.rehome(st);
+    }
+    TermsView view() const {
+        TermsView t;
+        t.n = n;
+        t.W = W;
+        t.R = R;
+        t.chi = chi;
+        t.G = G.p;
+        t.F = F.p;
+        t.M = M.p;
+        t.V = V.p;
+        t.S = S.p;
+        t.GL = GL.p;
+        t.GH = GH.p;
+        t.phase = phase.p;
+        t.coef_k = ck.p;
+        t.coef_r = cr.p;
+        return t;
+    }
+    void copy_from(const TermStore& o, cudaStream_t st) {
+        alloc(o.n, std::max<int64_t>(o.chi, 1), st);
+        W = o.W;
+        R = o.R;
+        chi = o.chi;
+        size_t rows = (size_t)chi * R * W, vec = (size_t)chi * W;
+        CK(cudaMemcpyAsync(G.p, o.G.p, rows * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(F.p, o.F.p, rows * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(M.p, o.M.p, rows * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(V.p, o.V.p, vec * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(S.p, o.S.p, vec * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(GL.p, o.GL.p, vec * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(GH.p, o.GH.p, vec * 8, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(phase.p, o.phase.p, chi, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(ck.p, o.ck.p, chi, cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(cr.p, o.cr.p, chi * 4, cudaMemcpyDeviceToDevice, st));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// |T⟩^{⊗t} expansion, cached per t (host) and per (device, t) (device).
+struct TTensorHost {
+    int t = 0;
+    int64_t chi = 0;
+    std::vector<uint64_t> G, F, M, V, S;
+    std::vector<uint8_t> gam, phase, ck;
+    std::vector<int32_t> cr;
+};
+
+// Device copy of the expansion; allocated once per (device, t) with plain
+// cudaMalloc and kept for the life of the process (never freed, so no CUDA
+// call runs from a static destructor).
+struct TTensorDev {
+    int64_t chi = 0;
+    uint64_t *G = nullptr, *F = nullptr, *M = nullptr, *V = nullptr, *S = nullptr;
+    uint8_t *gam = nullptr, *phase = nullptr, *ck = nullptr;
+    int32_t* cr = nullptr;
+};
+
+template <typename T>
+T* dev_copy(const std::vector<T>& h) {
+    T* p = nullptr;
+    size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void**)&p, bytes);
+    if (e == cudaErrorMemoryAllocation) raise(NSG_ERR_OUT_OF_MEMORY, (int64_t)bytes, -1, "device allocation failed");
+    cuda_check(e, "cudaMalloc");
+    if (!h.empty()) cuda_check(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+    return p;
+}
+
+std::mutex g_cache_mu;
+std::map<int, std::shared_ptr<TTensorHost>> g_tt_host;
+std::map<std::pair<int, int>, std::shared_ptr<TTensorDev>> g_tt_dev;
+
+std::shared_ptr<TTensorHost> t_tensor_host(int t) {
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        auto it = g_tt_host.find(t);
+        if (it != g_tt_host.end()) return it->second;
+    }
+    auto h = std::make_shared<TTensorHost>();
+    h->t = t;
+    if (t == 0) {  // the Clifford-only circuit: one term |0^n⟩ with coefficient 1
+        h->chi = 1;
+        h->G.assign(1, 0);
+        h->F.assign(1, 0);
+        h->M.assign(1, 0);
+        h->gam.assign(1, 0);
+        h->V.assign(1, 0);
+        h->S.assign(1, 0);
+        h->phase.assign(1, 0);
+        h->ck.assign(1, 0);
+        h->cr.assign(1, 0);
+    } else {
+        HostDecomp d;
+        try {
+            d = t_tensor_state(t);
+        } catch (const HostError& e) {
+            raise(NSG_ERR_DEVICE_INVARIANT, e.code, e.a, "T-state expansion failed (%d)", e.code);
+        }
+        h->chi = (int64_t)d.terms.size();
+        size_t rows = (size_t)h->chi * t;
+        h->G.resize(rows);
+        h->F.resize(rows);
+        h->M.resize(rows);
+        h->gam.resize(rows);
+        h->V.resize(h->chi);
+        h->S.resize(h->chi);
+        h->phase.resize(h->chi);
+        h->ck.resize(h->chi);
+        h->cr.resize(h->chi);
+        for (int64_t i = 0; i < h->chi; i++) {
+            const HostCH& c = d.terms[i];
+            for (int r = 0; r < t; r++) {
+                h->G[i * t + r] = c.G[r].w[0];
+                h->F[i * t + r] = c.F[r].w[0];
+                h->M[i * t + r] = c.M[r].w[0];
+                h->gam[i * t + r] = c.gam[r];
+            }
+            h->V[i] = c.v[0];
+            h->S[i] = c.s[0];
+            h->phase[i] = (uint8_t)c.phase;
+            h->ck[i] = (uint8_t)d.coef[i].k;
+            h->cr[i] = d.coef[i].r;
+        }
+    }
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_tt_host[t] = h;
+    return h;
+}
+
+std::shared_ptr<TTensorDev> t_tensor_dev(int t, cudaStream_t st) {
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    {
+        std::lock_guard<std::mutex> lk(g_cache_mu);
+        auto it = g_tt_dev.find({dev, t});
+        if (it != g_tt_dev.end()) return it->second;
+    }
+    auto h = t_tensor_host(t);
+    auto d = std::make_shared<TTensorDev>();
+    d->chi = h->chi;
+    CK(cudaStreamSynchronize(st));
+    d->G = dev_copy(h->G);
+    d->F = dev_copy(h->F);
+    d->M = dev_copy(h->M);
+    d->gam = dev_copy(h->gam);
+    d->V = dev_copy(h->V);
+    d->S = dev_copy(h->S);
+    d->phase = dev_copy(h->phase);
+    d->ck = dev_copy(h->ck);
+    d->cr = dev_copy(h->cr);
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_tt_dev[{dev, t}] = d;
+    return d;
+}
+
+// ---------------------------------------------------------------------------
+// Gate lowering with the reference's index checks.
+//
+// The reference checks indices when a gate is applied to a term
+// (form/left_multiplication/*.rs): one-qubit gates check q < n; CX/CZ check
+// control, then target, then equality; SWAP the same before its three CX;
+// SqrtX/SqrtXdg check through their first H.  For a circuit with T gates
+// the terms have width n+t during compilation (compiler/mod.rs:97-102).
+void lower_clifford(const nsg_gate& g, int width, std::vector<uint32_t>& out) {
+    auto chk1 = [&](uint32_t q) {
+        if ((int64_t)q >= width) err_oob(q, width);
+    };
+    auto chk2 = [&](uint32_t a, uint32_t b) {
+        chk1(a);
+        chk1(b);
+        if (a == b) err_dup_gate(a);
+    };
+    switch (g.op) {
+        case NSG_GATE_H: chk1(g.q0); out.push_back(enc_op(P_H, g.q0)); break;
+        case NSG_GATE_X: chk1(g.q0); out.push_back(enc_op(P_X, g.q0)); break;
+        case NSG_GATE_Y: chk1(g.q0); out.push_back(enc_op(P_Y, g.q0)); break;
+        case NSG_GATE_Z: chk1(g.q0); out.push_back(enc_op(P_Z, g.q0)); break;
+        case NSG_GATE_S: chk1(g.q0); out.push_back(enc_op(P_S, g.q0)); break;
+        case NSG_GATE_SDG: chk1(g.q0); out.push_back(enc_op(P_SDG, g.q0)); break;
+        case NSG_GATE_SQRT_X:  // sqrt_x.rs:6-10
+            chk1(g.q0);
+            out.push_back(enc_op(P_H, g.q0));
+            out.push_back(enc_op(P_S, g.q0));
+            out.push_back(enc_op(P_H, g.q0));
+            break;
+        case NSG_GATE_SQRT_XDG:  // sqrt_x.rs:12-16
+            chk1(g.q0);
+            out.push_back(enc_op(P_H, g.q0));
+            out.push_back(enc_op(P_SDG, g.q0));
+            out.push_back(enc_op(P_H, g.q0));
+            break;
+        case NSG_GATE_CX: chk2(g.q0, g.q1); out.push_back(enc_op(P_CX, g.q0, g.q1)); break;
+        case NSG_GATE_CZ: chk2(g.q0, g.q1); out.push_back(enc_op(P_CZ, g.q0, g.q1)); break;
+        case NSG_GATE_SWAP:  // swap.rs:7-24
+            chk2(g.q0, g.q1);
+            out.push_back(enc_op(P_CX, g.q0, g.q1));
+            out.push_back(enc_op(P_CX, g.q1, g.q0));
+            out.push_back(enc_op(P_CX, g.q0, g.q1));
+            break;
+        default:
+            raise(NSG_ERR_GATE_NOT_CLIFFORD, g.op, -1, "Attempted to convert a non-Clifford gate to a Clifford gate: %s",
+                  gate_name(g.op));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Pauli strings -> bit form.  apply_pauli (form/gate_application.rs:186-210)
+// multiplies the ops on from the left in list order; composing them here
+// keeps repeated qubits exact.
+DevPauli to_dev_pauli(const nsg_pauli& p, int n) {
+    if (p.kind == NSG_PAULI_DENSE) {  // exp_value.rs:9-17
+        if ((int)p.len != n)
+            raise(NSG_ERR_INVALID_PAULI_STRING_LENGTH, n, p.len, "Invalid Pauli string length: expected %d, found %u.", n,
+                  p.len);
+    } else if (p.kind == NSG_PAULI_SPARSE) {  // :18-26
+        uint32_t maxq = 0;
+        for (uint32_t i = 0; i < p.len; i++) maxq = std::max(maxq, p.qubits ? p.qubits[i] : 0u);
+        if ((int64_t)maxq >= n)
+            raise(NSG_ERR_INVALID_PAULI_STRING_LENGTH, n, (int64_t)maxq + 1,
+                  "Invalid Pauli string length: expected %d, found %u.", n, maxq + 1);
+    } else {
+        raise(NSG_ERR_INVALID_ARGUMENT, p.kind, -1, "invalid Pauli kind %u", p.kind);
+    }
+    if (p.len && !p.ops) raise(NSG_ERR_INVALID_ARGUMENT, -1, -1, "null Pauli ops");
+    if (p.kind == NSG_PAULI_SPARSE && p.len && !p.qubits) raise(NSG_ERR_INVALID_ARGUMENT, -1, -1, "null Pauli qubits");
+    DevPauli d{0, 0, 0, 0};
+    int e = 0;  // P = i^e X(px) Z(pz)
+    for (uint32_t i = 0; i < p.len; i++) {
+        uint32_t q = (p.kind == NSG_PAULI_DENSE) ? i : p.qubits[i];
+        uint8_t op = p.ops[i];
+        uint64_t bit = 1ULL << q;
+        int xq = (d.px >> q) & 1;
+        switch (op) {
+            case NSG_PAULI_I: break;
+            case NSG_PAULI_X: d.px ^= bit; break;                           // X_q·X(px)Z(pz)
+            case NSG_PAULI_Z: e += 2 * xq; d.pz ^= bit; break;              // Z_q X(px) = (-1)^{px_q} X(px) Z_q
+            case NSG_PAULI_Y: e += 1 + 2 * xq; d.px ^= bit; d.pz ^= bit; break;  // Y = iXZ
+            default: raise(NSG_ERR_INVALID_ARGUMENT, op, -1, "invalid Pauli op %u", op);
+        }
+    }
+    d.ny = e & 3;
+    return d;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct nsg_state {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t st = nullptr;
+    TermStore t;
+    double gf_re = 1.0, gf_im = 0.0;
+    // cached bra frames
+    bool frames_ok = false;
+    DBuf<uint64_t> fGV, fFV, fMV, fGVL, fGVH;
+    DBuf<int> status;
+
+    void init_stream() {
+        CK(cudaGetDevice(&device));
+        CK(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
+        st = own;
+        status.alloc(1, st);
+        CK(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+    }
+    ~nsg_state() {
+        // Finish work on the current stream, then free everything on our own.
+        if (st) cudaStreamSynchronize(st);
+        t.rehome(own);
+        fGV.rehome(own);
+        fFV.rehome(own);
+        fMV.rehome(own);
+        fGVL.rehome(own);
+        fGVH.rehome(own);
+        status.rehome(own);
+        t = TermStore();
+        fGV.release();
+        fFV.release();
+        fMV.release();
+        fGVL.release();
+        fGVH.release();
+        status.release();
+        if (own) {
+            cudaStreamSynchronize(own);
+            cudaStreamDestroy(own);
+        }
+    }
+    void invalidate() { frames_ok = false; }
+    FrameView frames() {
+        if (!frames_ok) {
+            size_t cap = (size_t)std::max<int64_t>(t.chi, 1);
+            fGV.alloc(cap * 64, st);
+            fFV.alloc(cap * 64, st);
+            fMV.alloc(cap * 64, st);
+            fGVL.alloc(cap, st);
+            fGVH.alloc(cap, st);
+            FrameView fr{fGV.p, fFV.p, fMV.p, fGVL.p, fGVH.p};
+            CK(launch_frames(t.view(), fr, st));
+            frames_ok = true;
+        }
+        return FrameView{fGV.p, fFV.p, fMV.p, fGVL.p, fGVH.p};
+    }
+    // Reads and clears the device status word; maps it to an API error.
+    void check_status(int64_t qubit = -1) {
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (h) {
+            CK(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+            CK(cudaStreamSynchronize(st));
+            if (h & DS_CANNOT_DISCARD)
+                raise(NSG_ERR_CANNOT_DISCARD_QUBIT, qubit, -1, "Cannot discard qubit %lld because it is not in a proper state",
+                      (long long)qubit);
+            raise(NSG_ERR_DEVICE_INVARIANT, h, -1, "device invariant violated (status %d)", h);
+        }
+    }
+};
+
+namespace {
+
+#define API_BEGIN try {
+#define API_END                               \
+    }                                         \
+    catch (const ApiError& e) { return e.code; } \
+    catch (const std::exception& e) {         \
+        g_msg = e.what();                     \
+        return NSG_ERR_INVALID_ARGUMENT;      \
+    }                                         \
+    return NSG_OK;
+
+void need(const void* p, const char* what) {
+    if (!p) raise(NSG_ERR_INVALID_ARGUMENT, -1, -1, "null %s", what);
+}
+
+void require_pairs_width(const nsg_state* s) {
+    if (s->t.n > 64) raise(NSG_ERR_TOO_WIDE, s->t.n, 64, "pair sums support at most 64 qubits, got %d", s->t.n);
+}
+
+// Replaces the terms of `s` by the kept ones (stable order).
+void compact_into(nsg_state* s, DBuf<int32_t>& keep) {
+    TermStore out;
+    out.alloc(s->t.n, std::max<int64_t>(s->t.chi, 1), s->st);
+    out.W = s->t.W;
+    out.R = s->t.R;
+    DBuf<int32_t> pos;
+    pos.alloc(std::max<int64_t>(s->t.chi, 1), s->st);
+    DBuf<int64_t> cnt;
+    cnt.alloc(1, s->st);
+    TermsView ov = out.view();
+    CK(launch_compact(s->t.view(), keep.p, pos.p, ov, cnt.p, s->st));
+    int64_t h = 0;
+    CK(cudaMemcpyAsync(&h, cnt.p, sizeof(int64_t), cudaMemcpyDeviceToHost, s->st));
+    CK(cudaStreamSynchronize(s->st));
+    out.chi = h;
+    s->t = std::move(out);
+    s->invalidate();
+}
+
+// Process-wide pair-kernel timing (nsg_profile_*).
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+double g_prof_ms = 0.0;
+uint64_t g_prof_launches = 0, g_prof_pairs = 0;
+
+// Σ-pairs driver: one launch over the pair space for `nobs` observables.
+void run_pairs(nsg_state* a, nsg_state* b, const std::vector<DevPauli>& paulis, bool triangular, bool complex_out,
+               bool mixed, std::vector<double>& out, uint8_t* dbg_k = nullptr, int32_t* dbg_r = nullptr) {
+    cudaStream_t st = a->st;
+    const int nobs = (int)paulis.size();
+    const int64_t chiA = a->t.chi, chiB = b->t.chi;
+    out.assign((size_t)nobs * (complex_out ? 2 : 1), 0.0);
+    if (nobs == 0 || chiA == 0 || chiB == 0) return;
+    FrameView fr = a->frames();
+    DBuf<DevPauli> dp;
+    dp.alloc(nobs, st);
+    CK(cudaMemcpyAsync(dp.p, paulis.data(), nobs * sizeof(DevPauli), cudaMemcpyHostToDevice, st));
+    DBuf<uint64_t> px;
+    DBuf<uint8_t> pk;
+    px.alloc((size_t)chiA * nobs, st);
+    pk.alloc((size_t)chiA * nobs, st);
+    CK(launch_pauli_frames(a->t.view(), dp.p, nobs, px.p, pk.p, st));
+
+    PairLaunch pl;
+    pl.A = a->t.view();
+    pl.fr = fr;
+    pl.B = b->t.view();
+    pl.px = px.p;
+    pl.pk = pk.p;
+    pl.nobs = nobs;
+    pl.triangular = triangular;
+    pl.complex_out = complex_out;
+    pl.mixed = mixed;
+    pl.chunk = 32;
+    std::vector<int64_t> off;
+    DBuf<int64_t> doff;
+    if (triangular) {
+        off.resize(chiA + 1);
+        off[0] = 0;
+        for (int64_t i = 0; i < chiA; i++) off[i + 1] = off[i] + (chiA - i + pl.chunk - 1) / pl.chunk;
+        pl.total_chunks = off[chiA];
+        doff.alloc(off.size(), st);
+        CK(cudaMemcpyAsync(doff.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, st));
+        pl.row_chunk_off = doff.p;
+    } else {
+        pl.total_chunks = chiA * ((chiB + pl.chunk - 1) / pl.chunk);
+    }
+    const int sms = device_sm_count();
+    const int wpb = 4;
+    int64_t want_blocks = (pl.total_chunks + wpb - 1) / wpb;
+    pl.blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want_blocks, (int64_t)sms * 16));
+    pl.warps_per_block = wpb;
+    pl.nwarps = pl.blocks * wpb;
+    DBuf<double> partials;
+    partials.alloc((size_t)pl.nwarps * nobs * 8, st);
+    CK(cudaMemsetAsync(partials.p, 0, partials.n * sizeof(double), st));
+    pl.partials = partials.p;
+    pl.status = a->status.p;
+    pl.dbg_k = dbg_k;
+    pl.dbg_r = dbg_r;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool prof;
+    {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        prof = g_prof_on;
+    }
+    if (prof) {
+        CK(cudaEventCreate(&ev0));
+        CK(cudaEventCreate(&ev1));
+        CK(cudaEventRecord(ev0, st));
+    }
+    CK(launch_pairs(pl, st));
+    if (prof) {
+        CK(cudaEventRecord(ev1, st));
+        CK(cudaEventSynchronize(ev1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, ev0, ev1));
+        cudaEventDestroy(ev0);
+        cudaEventDestroy(ev1);
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        g_prof_ms += ms;
+        g_prof_launches += 1;
+        g_prof_pairs += triangular ? (uint64_t)(chiA * (chiA + 1) / 2) : (uint64_t)(chiA * chiB);
+    }
+    double sre, sim;
+    if (complex_out) {  // conj(g_a)·g_b (stabilizer_decomposed_state/inner_product.rs:18)
+        sre = a->gf_re * b->gf_re + a->gf_im * b->gf_im;
+        sim = a->gf_re * b->gf_im - a->gf_im * b->gf_re;
+    } else {  // |g|² (exp_value.rs:60, norm.rs:29)
+        sre = a->gf_re * a->gf_re + a->gf_im * a->gf_im;
+        sim = 0.0;
+    }
+    DBuf<double> dout;
+    dout.alloc(out.size(), st);
+    CK(launch_reduce(partials.p, pl.nwarps, nobs, complex_out, sre, sim, dout.p, st));
+    CK(cudaMemcpyAsync(out.data(), dout.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    a->check_status();
+}
+
+double norm_squared(nsg_state* s) {
+    require_pairs_width(s);
+    std::vector<DevPauli> id(1, DevPauli{0, 0, 0, 0});
+    std::vector<double> out;
+    run_pairs(s, s, id, true, false, false, out);
+    return out[0];
+}
+
+void validate_qargs(const nsg_state* s, const uint32_t* q, size_t k) {  // stabilizer_decomposed_state/mod.rs:44-67
+    if (k == 0) raise(NSG_ERR_EMPTY_QUBIT_INDICES, -1, -1, "Qubit index list is empty.");
+    for (size_t i = 0; i < k; i++)
+        if ((int)q[i] >= s->t.n) err_oob(q[i], s->t.n);
+    std::vector<uint32_t> sorted(q, q + k);
+    std::sort(sorted.begin(), sorted.end());
+    for (size_t i = 1; i < k; i++)
+        if (sorted[i] == sorted[i - 1])
+            raise(NSG_ERR_DUPLICATE_QUBIT_INDEX, sorted[i], -1, "Duplicate qubit index found: %u.", sorted[i]);
+}
+
+void project_unnorm(nsg_state* s, uint32_t q, bool outcome) {  // projection.rs:27-57
+    if ((int)q >= s->t.n) err_oob(q, s->t.n);
+    DBuf<int32_t> keep;
+    keep.alloc(std::max<int64_t>(s->t.chi, 1), s->st);
+    CK(launch_project(s->t.view(), (int)q, outcome ? 1 : 0, keep.p, s->status.p, s->st));
+    s->check_status();
+    compact_into(s, keep);
+}
+
+void discard_q(nsg_state* s, uint32_t q) {  // discard.rs:5-12
+    if ((int)q >= s->t.n) err_oob(q, s->t.n);
+    CK(launch_discard(s->t.view(), (int)q, s->status.p, s->st));
+    s->check_status(q);
+    s->t.n -= 1;
+    s->invalidate();
+}
+
+void apply_ops(nsg_state* s, const std::vector<uint32_t>& ops) {
+    if (ops.empty() || s->t.chi == 0) return;
+    DBuf<uint32_t> d;
+    d.alloc(ops.size(), s->st);
+    CK(cudaMemcpyAsync(d.p, ops.data(), ops.size() * 4, cudaMemcpyHostToDevice, s->st));
+    CK(launch_apply_ops(d.p, (int)ops.size(), s->t.view(), s->status.p, s->st));
+    s->check_status();
+    s->invalidate();
+}
+
+nsg_state* clone_state(const nsg_state* s) {
+    auto* c = new nsg_state();
+    c->init_stream();
+    CK(cudaStreamSynchronize(s->st));
+    c->t.copy_from(s->t, c->st);
+    c->gf_re = s->gf_re;
+    c->gf_im = s->gf_im;
+    CK(cudaStreamSynchronize(c->st));
+    return c;
+}
+
+// Probabilities of outcome 0/1 of qubit q (unnormalised): ⟨ψ|(I±Z_q)/2|ψ⟩,
+// identical to norm_squared of the two projected states
+// (measurement.rs:35-65, sampling.rs:103-153) from one pass over the pairs.
+void outcome_weights(nsg_state* s, uint32_t q, double& w0, double& w1) {
+    require_pairs_width(s);
+    std::vector<DevPauli> ps(2, DevPauli{0, 0, 0, 0});
+    ps[1].pz = 1ULL << q;
+    std::vector<double> out;
+    run_pairs(s, s, ps, true, false, false, out);
+    w0 = 0.5 * (out[0] + out[1]);
+    w1 = 0.5 * (out[0] - out[1]);
+    if (w0 < 0.0) w0 = 0.0;
+    if (w1 < 0.0) w1 = 0.0;
+}
+
+struct ShotOut {
+    uint64_t lo, hi, count;
+};
+
+// recursive_sample (sampling.rs:80-189) with the binomial split of the
+// reference and the same descending qubit order.
+void sample_rec(nsg_state* s, const std::vector<std::pair<uint32_t, uint32_t>>& qs, size_t idx, uint64_t shots,
+                uint64_t lo, uint64_t hi, HostRng& rng, std::vector<ShotOut>& out) {
+    if (shots == 0) return;
+    if (idx == qs.size()) {
+        out.push_back({lo, hi, shots});
+        return;
+    }
+    uint32_t q = qs[idx].first, bit = qs[idx].second;
+    double w0, w1;
+    outcome_weights(s, q, w0, w1);
+    double tot = w0 + w1;
+    double p0 = tot > 0 ? std::min(1.0, std::max(0.0, w0 / tot)) : 0.0;
+    uint64_t n0 = rng.binomial(shots, p0), n1 = shots - n0;
+    if (n0 > 0) {
+        std::unique_ptr<nsg_state> z(n1 > 0 ? clone_state(s) : nullptr);
+        nsg_state* zz = z ? z.get() : s;
+        project_unnorm(zz, q, false);
+        discard_q(zz, q);
+        sample_rec(zz, qs, idx + 1, n0, lo, hi, rng, out);
+    }
+    if (n1 > 0) {
+        nsg_state* oo = s;  // the 0-branch worked on a clone when both are taken
+        project_unnorm(oo, q, true);
+        std::vector<uint32_t> xo{enc_op(P_X, q)};
+        apply_ops(oo, xo);  // |1⟩ -> |0⟩ before discarding (sampling.rs:175-176)
+        discard_q(oo, q);
+        uint64_t nlo = lo, nhi = hi;
+        if (bit < 64) nlo |= 1ULL << bit;
+        else nhi |= 1ULL << (bit - 64);
+        sample_rec(oo, qs, idx + 1, n1, nlo, nhi, rng, out);
+    }
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* nsg_version(void) { return "necstar-gb300 0.1"; }
+
+const char* nsg_last_error_message(void) { return g_msg.c_str(); }
+
+nsg_status nsg_last_error_args(int64_t out[3]) {
+    if (!out) return NSG_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < 3; i++) out[i] = g_args[i];
+    return NSG_OK;
+}
+
+nsg_status nsg_state_from_circuit(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates, nsg_state** out) {
+    API_BEGIN
+    need(out, "out");
+    *out = nullptr;
+    if (num_gates) need(gates, "gates");
+    const int n = (int)num_qubits;
+    // Lowering (compiler/mod.rs:49-63): T/Tdg -> CX(target, n+k) [+ Sdg(target)].
+    int t = 0;
+    for (size_t i = 0; i < num_gates; i++) {
+        uint32_t op = gates[i].op;
+        if (op == NSG_GATE_T || op == NSG_GATE_TDG) t++;
+        else if (op > NSG_GATE_SWAP)
+            raise(NSG_ERR_GATE_NOT_SUPPORTED, op, -1, "Gate %s is not supported.", gate_name(op));
+    }
+    if (n == 0) raise(NSG_ERR_INVALID_NUM_QUBITS, 0, -1, "Number of qubits must be greater than zero, got 0.");
+    const int width = n + t;
+    if (width > 128 || t > 64)
+        raise(NSG_ERR_TOO_WIDE, width, 128, "compilation width %d (n=%d, t=%d) exceeds the supported 128 (t <= 64)",
+              width, n, t);
+    std::vector<uint32_t> ops;
+    ops.reserve(num_gates + t);
+    int k = 0;
+    for (size_t i = 0; i < num_gates; i++) {
+        const nsg_gate& g = gates[i];
+        if (g.op == NSG_GATE_T || g.op == NSG_GATE_TDG) {
+            nsg_gate cx{NSG_GATE_CX, g.q0, (uint32_t)(n + k), 0};
+            lower_clifford(cx, width, ops);
+            if (g.op == NSG_GATE_TDG) {
+                nsg_gate sdg{NSG_GATE_SDG, g.q0, 0, 0};
+                lower_clifford(sdg, width, ops);
+            }
+            k++;
+        } else {
+            lower_clifford(g, width, ops);
+        }
+    }
+    auto s = std::make_unique<nsg_state>();
+    s->init_stream();
+    cudaStream_t st = s->st;
+    auto tt = t_tensor_dev(t, st);
+    DBuf<uint32_t> dops;
+    dops.alloc(std::max<size_t>(ops.size(), 1), st);
+    if (!ops.empty()) CK(cudaMemcpyAsync(dops.p, ops.data(), ops.size() * 4, cudaMemcpyHostToDevice, st));
+    TermStore raw;
+    raw.alloc(n, tt->chi, st);
+    raw.chi = tt->chi;
+    DBuf<int32_t> keep;
+    keep.alloc(tt->chi, st);
+    TermsView rv = raw.view();
+    CK(launch_compile(dops.p, (int)ops.size(), n, t, tt->chi, tt->G, tt->F, tt->M, tt->gam, tt->V, tt->S, tt->phase,
+                      tt->ck, tt->cr, rv, keep.p, s->status.p, st));
+    s->t = std::move(raw);
+    s->check_status();
+    compact_into(s.get(), keep);
+    *out = s.release();
+    API_END
+}
+
+nsg_status nsg_state_from_terms(uint32_t num_qubits, uint64_t num_terms, const uint8_t* G, const uint8_t* F,
+                                const uint8_t* M, const uint8_t* gamma, const uint8_t* v, const uint8_t* s_,
+                                const uint8_t* phase, const uint8_t* coef_phase, const int32_t* coef_r,
+                                const uint8_t* coef_zero, const double global_factor[2], nsg_state** out) {
+    API_BEGIN
+    need(out, "out");
+    *out = nullptr;
+    const int n = (int)num_qubits;
+    if (n > 128) raise(NSG_ERR_TOO_WIDE, n, 128, "width %d exceeds 128", n);
+    if (num_terms) {
+        need(G, "G"); need(F, "F"); need(M, "M"); need(gamma, "gamma"); need(v, "v"); need(s_, "s");
+        need(phase, "phase"); need(coef_phase, "coef_phase"); need(coef_r, "coef_r");
+    }
+    if (coef_zero)
+        for (uint64_t i = 0; i < num_terms; i++)
+            if (coef_zero[i]) raise(NSG_ERR_NOT_IMPLEMENTED, (int64_t)i, -1, "Not implemented: zero coefficients");
+    auto st_ = std::make_unique<nsg_state>();
+    st_->init_stream();
+    cudaStream_t st = st_->st;
+    st_->t.alloc(n, (int64_t)num_terms, st);
+    st_->t.chi = (int64_t)num_terms;
+    const size_t nn = (size_t)n * n * num_terms, nv = (size_t)n * num_terms;
+    DBuf<uint8_t> dG, dF, dM, dg, dv, ds;
+    if (num_terms && n) {
+        dG.alloc(nn, st); dF.alloc(nn, st); dM.alloc(nn, st);
+        dg.alloc(nv, st); dv.alloc(nv, st); ds.alloc(nv, st);
+        CK(cudaMemcpyAsync(dG.p, G, nn, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dF.p, F, nn, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dM.p, M, nn, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dg.p, gamma, nv, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(dv.p, v, nv, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(ds.p, s_, nv, cudaMemcpyHostToDevice, st));
+        CK(launch_pack(st_->t.view(), dG.p, dF.p, dM.p, dg.p, dv.p, ds.p, st));
+    }
+    if (num_terms) {
+        CK(cudaMemcpyAsync(st_->t.phase.p, phase, num_terms, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(st_->t.ck.p, coef_phase, num_terms, cudaMemcpyHostToDevice, st));
+        CK(cudaMemcpyAsync(st_->t.cr.p, coef_r, num_terms * 4, cudaMemcpyHostToDevice, st));
+    }
+    if (global_factor) {
+        st_->gf_re = global_factor[0];
+        st_->gf_im = global_factor[1];
+    }
+    CK(cudaStreamSynchronize(st));
+    *out = st_.release();
+    API_END
+}
+
+void nsg_state_free(nsg_state* state) { delete state; }
+
+nsg_status nsg_state_clone(const nsg_state* state, nsg_state** out) {
+    API_BEGIN
+    need(state, "state");
+    need(out, "out");
+    *out = clone_state(state);
+    API_END
+}
+
+nsg_status nsg_num_qubits(const nsg_state* state, uint32_t* out) {
+    API_BEGIN
+    need(state, "state");
+    need(out, "out");
+    *out = (uint32_t)state->t.n;
+    API_END
+}
+
+nsg_status nsg_stabilizer_rank(const nsg_state* state, uint64_t* out) {
+    API_BEGIN
+    need(state, "state");
+    need(out, "out");
+    *out = (uint64_t)state->t.chi;
+    API_END
+}
+
+nsg_status nsg_state_set_stream(nsg_state* state, void* cuda_stream) {
+    API_BEGIN
+    need(state, "state");
+    CK(cudaStreamSynchronize(state->st));
+    state->st = cuda_stream ? (cudaStream_t)cuda_stream : state->own;
+    // Buffers are freed on the stream that last uses them.
+    state->t.rehome(state->st);
+    state->fGV.rehome(state->st);
+    state->fFV.rehome(state->st);
+    state->fMV.rehome(state->st);
+    state->fGVL.rehome(state->st);
+    state->fGVH.rehome(state->st);
+    state->status.rehome(state->st);
+    API_END
+}
+
+nsg_status nsg_apply_gates(nsg_state* state, const nsg_gate* gates, size_t num_gates) {
+    API_BEGIN
+    need(state, "state");
+    if (num_gates) need(gates, "gates");
+    // apply_gates (stabilizer_decomposed_state/gates.rs:7-37): gates apply in
+    // order; the first failing gate stops after its predecessors took effect.
+    // Index checks happen inside the per-term loop, so with no terms only
+    // non-Clifford gates fail.
+    std::vector<uint32_t> ops;
+    ApiError pending{NSG_OK};
+    std::string pmsg;
+    int64_t pargs[3] = {-1, -1, -1};
+    for (size_t i = 0; i < num_gates; i++) {
+        const nsg_gate& g = gates[i];
+        if (g.op > NSG_GATE_SWAP) {
+            if (g.op > NSG_GATE_CCX) {
+                pending = ApiError{NSG_ERR_INVALID_ARGUMENT};
+                pmsg = "invalid gate opcode";
+            } else {
+                pending = ApiError{NSG_ERR_NON_CLIFFORD_GATE_APPLICATION};
+                pmsg = std::string("Direct application of non-Clifford gate ") + gate_name(g.op) + " is not supported.";
+                pargs[0] = g.op;
+            }
+            break;
+        }
+        if (state->t.chi == 0) continue;
+        try {
+            lower_clifford(g, state->t.n, ops);
+        } catch (const ApiError& e) {
+            pending = e;
+            pmsg = g_msg;
+            for (int j = 0; j < 3; j++) pargs[j] = g_args[j];
+            break;
+        }
+    }
+    apply_ops(state, ops);
+    if (pending.code != NSG_OK) {
+        g_msg = pmsg;
+        for (int j = 0; j < 3; j++) g_args[j] = pargs[j];
+        return pending.code;
+    }
+    API_END
+}
+
+nsg_status nsg_exp_value(const nsg_state* state, const nsg_pauli* pauli, double* out) {
+    return nsg_exp_value_batch(state, pauli, 1, NSG_PRECISION_FP64, out);
+}
+
+nsg_status nsg_exp_value_batch(const nsg_state* cstate, const nsg_pauli* paulis, size_t num_paulis,
+                               uint32_t precision, double* out) {
+    API_BEGIN
+    need(cstate, "state");
+    if (num_paulis) {
+        need(paulis, "paulis");
+        need(out, "out");
+    }
+    if (precision > NSG_PRECISION_MIXED) raise(NSG_ERR_INVALID_ARGUMENT, precision, -1, "invalid precision");
+    nsg_state* state = const_cast<nsg_state*>(cstate);
+    require_pairs_width(state);
+    std::vector<DevPauli> dp(num_paulis);
+    for (size_t i = 0; i < num_paulis; i++) dp[i] = to_dev_pauli(paulis[i], state->t.n);
+    const size_t per = 256;  // observables per pass (8 lane groups)
+    for (size_t base = 0; base < num_paulis; base += per) {
+        size_t cnt = std::min(per, num_paulis - base);
+        std::vector<DevPauli> part(dp.begin() + base, dp.begin() + base + cnt);
+        std::vector<double> r;
+        run_pairs(state, state, part, true, false, precision == NSG_PRECISION_MIXED, r);
+        std::memcpy(out + base, r.data(), cnt * sizeof(double));
+    }
+    API_END
+}
+
+nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states, const nsg_pauli* paulis,
+                               const uint64_t* pauli_offsets, uint32_t precision, double* out) {
+    API_BEGIN
+    need(pauli_offsets, "pauli_offsets");
+    if (num_states) need(states, "states");
+    for (size_t c = 0; c < num_states; c++) {
+        uint64_t b = pauli_offsets[c], e = pauli_offsets[c + 1];
+        if (e < b) raise(NSG_ERR_INVALID_ARGUMENT, (int64_t)c, -1, "pauli_offsets not ascending");
+        nsg_status rc = nsg_exp_value_batch(states[c], paulis + b, (size_t)(e - b), precision, out + b);
+        if (rc != NSG_OK) return rc;
+    }
+    API_END
+}
+
+nsg_status nsg_inner_product(const nsg_state* a, const nsg_state* b, double out[2]) {
+    API_BEGIN
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    if (a->t.n != b->t.n)
+        raise(NSG_ERR_QUBIT_COUNT_MISMATCH, a->t.n, b->t.n,
+              "The qubit counts of the two states must match for calculating inner product, got %d and %d.", a->t.n,
+              b->t.n);
+    nsg_state* aa = const_cast<nsg_state*>(a);
+    nsg_state* bb = const_cast<nsg_state*>(b);
+    require_pairs_width(aa);
+    if (aa != bb) CK(cudaStreamSynchronize(bb->st));
+    std::vector<DevPauli> id(1, DevPauli{0, 0, 0, 0});
+    std::vector<double> r;
+    run_pairs(aa, bb, id, false, true, false, r);
+    out[0] = r[0];
+    out[1] = r[1];
+    API_END
+}
+
+nsg_status nsg_norm(const nsg_state* state, double* out) {
+    API_BEGIN
+    need(state, "state");
+    need(out, "out");
+    *out = std::sqrt(norm_squared(const_cast<nsg_state*>(state)));
+    API_END
+}
+
+nsg_status nsg_project_unnormalized(nsg_state* state, uint32_t qubit, int32_t outcome) {
+    API_BEGIN
+    need(state, "state");
+    project_unnorm(state, qubit, outcome != 0);
+    API_END
+}
+
+nsg_status nsg_project_normalized(nsg_state* state, uint32_t qubit, int32_t outcome) {
+    API_BEGIN
+    need(state, "state");
+    project_unnorm(state, qubit, outcome != 0);  // projection.rs:10-21
+    double nrm = std::sqrt(norm_squared(state));
+    if (std::fabs(nrm) < 1e-12 || std::isnan(nrm)) err_impossible(qubit, outcome != 0);
+    state->gf_re /= nrm;
+    state->gf_im /= nrm;
+    API_END
+}
+
+nsg_status nsg_discard(nsg_state* state, uint32_t qubit) {
+    API_BEGIN
+    need(state, "state");
+    discard_q(state, qubit);
+    API_END
+}
+
+nsg_status nsg_measure(nsg_state* state, const uint32_t* qargs, size_t num_qargs, const uint8_t* seed32,
+                       uint8_t* out) {
+    API_BEGIN
+    need(state, "state");
+    if (num_qargs) {
+        need(qargs, "qargs");
+        need(out, "out");
+    }
+    validate_qargs(state, qargs, num_qargs);
+    HostRng rng(seed32);
+    for (size_t i = 0; i < num_qargs; i++) {  // measurement.rs:34-103
+        uint32_t q = qargs[i];
+        double p0, p1;
+        outcome_weights(state, q, p0, p1);
+        double tot = p0 + p1;
+        if (std::fabs(tot) < 1e-12)
+            raise(NSG_ERR_NOT_IMPLEMENTED, -1, -1, "Not implemented: Measurement on a zero-norm state is not possible.");
+        double u = rng.uniform();
+        bool one = !(u < p0 / tot);
+        double nsq = one ? p1 : p0;
+        double nrm = std::sqrt(nsq);
+        if (std::fabs(nrm) < 1e-12)
+            raise(NSG_ERR_NOT_IMPLEMENTED, -1, -1,
+                  "Not implemented: Measurement resulted in a zero-norm state, which is not physical.");
+        project_unnorm(state, q, one);
+        state->gf_re /= nrm;
+        state->gf_im /= nrm;
+        out[i] = one ? 1 : 0;
+    }
+    API_END
+}
+
+nsg_status nsg_measure_all(nsg_state* state, const uint8_t* seed32, uint8_t* out) {
+    API_BEGIN
+    need(state, "state");
+    std::vector<uint32_t> q(state->t.n);
+    for (int i = 0; i < state->t.n; i++) q[i] = i;
+    nsg_status rc = nsg_measure(state, q.data(), q.size(), seed32, out);
+    if (rc != NSG_OK) return rc;
+    API_END
+}
+
+nsg_status nsg_sample(const nsg_state* cstate, const uint32_t* qargs, size_t num_qargs, uint64_t shots,
+                      const uint8_t* seed32, uint64_t* outcomes, uint64_t* counts, size_t capacity,
+                      size_t* num_out) {
+    API_BEGIN
+    need(cstate, "state");
+    need(num_out, "num_out");
+    nsg_state* state = const_cast<nsg_state*>(cstate);
+    if (num_qargs) need(qargs, "qargs");
+    validate_qargs(state, qargs, num_qargs);
+    if (num_qargs > 128) raise(NSG_ERR_SAMPLING_TOO_MANY_QUBITS, -1, -1, "Sampling more than 128 qubits is not supported.");
+    HostRng rng(seed32);
+    std::vector<std::pair<uint32_t, uint32_t>> qs;  // (qarg, bit), descending qarg (sampling.rs:31-37)
+    for (size_t i = 0; i < num_qargs; i++) qs.push_back({qargs[i], (uint32_t)i});
+    std::stable_sort(qs.begin(), qs.end(), [](auto& a, auto& b) { return a.first > b.first; });
+    std::unique_ptr<nsg_state> work(clone_state(state));
+    std::vector<ShotOut> res;
+    sample_rec(work.get(), qs, 0, shots, 0, 0, rng, res);
+    *num_out = res.size();
+    if (res.size() > capacity)
+        raise(NSG_ERR_BUFFER_TOO_SMALL, (int64_t)res.size(), (int64_t)capacity,
+              "sample needs room for %zu outcomes, got %zu", res.size(), capacity);
+    for (size_t i = 0; i < res.size(); i++) {
+        outcomes[2 * i] = res[i].lo;
+        outcomes[2 * i + 1] = res[i].hi;
+        counts[i] = res[i].count;
+    }
+    API_END
+}
+
+nsg_status nsg_to_statevector(const nsg_state* state, double* out, size_t capacity_complex) {
+    API_BEGIN
+    need(state, "state");
+    const int n = state->t.n;
+    if (n > 28)
+        raise(NSG_ERR_STATEVECTOR_TOO_LARGE, n, -1,
+              "Calculating the statevector for a state with %d qubits is not feasible.", n);
+    if (n > 64) raise(NSG_ERR_TOO_WIDE, n, 64, "too wide");
+    size_t dim = (size_t)1 << n;
+    need(out, "out");
+    if (capacity_complex < dim)
+        raise(NSG_ERR_BUFFER_TOO_SMALL, (int64_t)dim, (int64_t)capacity_complex, "statevector needs %zu entries", dim);
+    cudaStream_t st = state->st;
+    DBuf<double> d;
+    d.alloc(2 * dim, st);
+    CK(launch_statevector(state->t.view(), state->gf_re, state->gf_im, d.p, st));
+    CK(cudaMemcpyAsync(out, d.p, 2 * dim * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    API_END
+}
+
+nsg_status nsg_export_terms(const nsg_state* state, uint8_t* G, uint8_t* F, uint8_t* M, uint8_t* gamma, uint8_t* v,
+                            uint8_t* s, uint8_t* phase, uint8_t* coef_phase, int32_t* coef_r, uint8_t* coef_zero,
+                            double global_factor[2]) {
+    API_BEGIN
+    need(state, "state");
+    cudaStream_t st = state->st;
+    const int64_t chi = state->t.chi;
+    const int n = state->t.n;
+    const size_t nn = (size_t)n * n * chi, nv = (size_t)n * chi;
+    if (chi && n) {
+        need(G, "G"); need(F, "F"); need(M, "M"); need(gamma, "gamma"); need(v, "v"); need(s, "s");
+        DBuf<uint8_t> dG, dF, dM, dg, dv, ds;
+        dG.alloc(nn, st); dF.alloc(nn, st); dM.alloc(nn, st);
+        dg.alloc(nv, st); dv.alloc(nv, st); ds.alloc(nv, st);
+        CK(launch_unpack(state->t.view(), dG.p, dF.p, dM.p, dg.p, dv.p, ds.p, st));
+        CK(cudaMemcpyAsync(G, dG.p, nn, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(F, dF.p, nn, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(M, dM.p, nn, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(gamma, dg.p, nv, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(v, dv.p, nv, cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(s, ds.p, nv, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    if (chi) {
+        if (phase) CK(cudaMemcpyAsync(phase, state->t.phase.p, chi, cudaMemcpyDeviceToHost, st));
+        if (coef_phase) CK(cudaMemcpyAsync(coef_phase, state->t.ck.p, chi, cudaMemcpyDeviceToHost, st));
+        if (coef_r) CK(cudaMemcpyAsync(coef_r, state->t.cr.p, chi * 4, cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (coef_zero) std::memset(coef_zero, 0, chi);
+    }
+    if (global_factor) {
+        global_factor[0] = state->gf_re;
+        global_factor[1] = state->gf_im;
+    }
+    API_END
+}
+
+nsg_status nsg_profile_enable(int32_t enabled) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    g_prof_on = enabled != 0;
+    return NSG_OK;
+}
+
+nsg_status nsg_profile_read(double* pair_kernel_ms, uint64_t* launches, uint64_t* pairs) {
+    std::lock_guard<std::mutex> lk(g_prof_mu);
+    if (pair_kernel_ms) *pair_kernel_ms = g_prof_ms;
+    if (launches) *launches = g_prof_launches;
+    if (pairs) *pairs = g_prof_pairs;
+    g_prof_ms = 0.0;
+    g_prof_launches = 0;
+    g_prof_pairs = 0;
+    return NSG_OK;
+}
+
+nsg_status nsg_probe_int_ops(uint64_t iters, double* seconds, uint64_t* ops) {
+    API_BEGIN
+    need(seconds, "seconds");
+    need(ops, "ops");
+    cudaStream_t st;
+    CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const int sms = device_sm_count(), threads = 256, blocks = sms * 8;
+    uint32_t* sink = nullptr;
+    CK(cudaMalloc((void**)&sink, blocks * sizeof(uint32_t)));
+    CK(launch_int_probe(2, blocks, threads, sink, st));  // warm-up
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, st));
+    CK(launch_int_probe(iters, blocks, threads, sink, st));
+    CK(cudaEventRecord(e1, st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    cudaStreamDestroy(st);
+    *seconds = ms * 1e-3;
+    *ops = (uint64_t)blocks * threads * iters * 16 * 8;
+    API_END
+}
+
+nsg_status nsg_debug_pair_values(const nsg_state* cstate, const nsg_pauli* pauli, uint8_t* k, int32_t* r) {
+    API_BEGIN
+    need(cstate, "state");
+    need(k, "k");
+    need(r, "r");
+    nsg_state* state = const_cast<nsg_state*>(cstate);
+    require_pairs_width(state);
+    std::vector<DevPauli> dp(1, DevPauli{0, 0, 0, 0});
+    if (pauli) dp[0] = to_dev_pauli(*pauli, state->t.n);
+    const int64_t chi = state->t.chi;
+    if (chi == 0) return NSG_OK;
+    DBuf<uint8_t> dk;
+    DBuf<int32_t> dr;
+    dk.alloc((size_t)chi * chi, state->st);
+    dr.alloc((size_t)chi * chi, state->st);
+    std::vector<double> out;
+    run_pairs(state, state, dp, false, true, false, out, dk.p, dr.p);
+    CK(cudaMemcpyAsync(k, dk.p, (size_t)chi * chi, cudaMemcpyDeviceToHost, state->st));
+    CK(cudaMemcpyAsync(r, dr.p, (size_t)chi * chi * 4, cudaMemcpyDeviceToHost, state->st));
+    CK(cudaStreamSynchronize(state->st));
+    API_END
+}
+
+}  // extern "C"

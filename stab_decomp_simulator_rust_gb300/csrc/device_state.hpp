@@ -1,0 +1,151 @@
+// device_state.hpp — the HBM layout of a stabilizer-decomposed state and the
+// launchers of the kernels that operate on it.
+//
+// Terms are stored structure-of-arrays.  A term of width n uses W = ⌈n/64⌉
+// 64-bit words per row and R = 64·W row slots, so lane l of a warp reads rows
+// l, l+32, ... of one term as contiguous 8·W-byte chunks (coalesced):
+//   G, F, M   [cap][R][W]   tableau rows (row r, column c = bit c)
+//   V, S      [cap][W]      the bit vectors v, s
+//   GL, GH    [cap][W]      γ as two bit planes: γ_r = GL_r + 2·GH_r (power of i)
+//   phase     [cap]         Z8 exponent of the CH-form phase factor
+//   coef_k    [cap]         Z8 phase of the exact coefficient
+//   coef_r    [cap]         its exponent: coefficient = e^{iπk/4}·2^{-r/2}
+// The reference's ω is 1 on every path (form/kron.rs:55 and
+// form/mod.rs:76-81 are its only writers) and is not stored.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace nsg {
+
+struct TermsView {
+    int n = 0;        // width
+    int W = 1;        // words per row
+    int R = 64;       // row slots per term
+    int64_t chi = 0;  // number of terms
+    uint64_t* G = nullptr;
+    uint64_t* F = nullptr;
+    uint64_t* M = nullptr;
+    uint64_t* V = nullptr;
+    uint64_t* S = nullptr;
+    uint64_t* GL = nullptr;
+    uint64_t* GH = nullptr;
+    uint8_t* phase = nullptr;
+    uint8_t* coef_k = nullptr;
+    int32_t* coef_r = nullptr;
+};
+
+// Per-term "bra frame": the tableau of U_C^{-1} (rows G_V, F_V, M_V, γ_V)
+// used by the pair kernel; W = 1 only (n ≤ 64).
+struct FrameView {
+    uint64_t* GV = nullptr;  // [chi][64]
+    uint64_t* FV = nullptr;
+    uint64_t* MV = nullptr;
+    uint64_t* GVL = nullptr;  // [chi] γ_V planes
+    uint64_t* GVH = nullptr;
+};
+
+// Pauli observable in bit form (n ≤ 64): P = i^{ny}·X(px)·Z(pz).
+struct DevPauli {
+    uint64_t px, pz;
+    int32_t ny;
+    int32_t pad;
+};
+
+// Encoded primitive gate: op | q0 << 8 | q1 << 16.
+enum PrimOp : uint32_t {
+    P_H = 0, P_X = 1, P_Y = 2, P_Z = 3, P_S = 4, P_SDG = 5, P_CX = 8, P_CZ = 9
+};
+inline uint32_t enc_op(uint32_t op, uint32_t a, uint32_t b = 0) { return op | (a << 8) | (b << 16); }
+
+// Device status word bits set by kernels (never a trap).
+enum DevStatus : int {
+    DS_OK = 0,
+    DS_INVARIANT = 1,  // reference panic paths
+    DS_CANNOT_DISCARD = 2,
+};
+
+// ---- launchers (kernels_*.cu) ------------------------------------------------
+
+// Compile: build |0^n⟩⊗T-term, apply the primitive op list, post-select the t
+// ancillas (reverse order) and discard them.  T-terms have width t ≤ 64 in
+// one word per row.  Writes unpacked results to `out` at the term's index and
+// keep[i] (1 kept, 0 dropped) and ndet[i].
+cudaError_t launch_compile(const uint32_t* d_ops, int nops, int n, int t, int64_t chi_t,
+                           const uint64_t* tG, const uint64_t* tF, const uint64_t* tM,
+                           const uint8_t* tGam, const uint64_t* tV, const uint64_t* tS,
+                           const uint8_t* tPhase, const uint8_t* tCk, const int32_t* tCr,
+                           TermsView out, int32_t* keep, int* status, cudaStream_t st);
+
+// Stable compaction of kept terms from `in` into `out` (same n/W); returns the
+// number kept through *d_count (device).  keep[] is consumed as 0/1 flags.
+cudaError_t launch_compact(const TermsView& in, const int32_t* keep, int32_t* scan_tmp,
+                           TermsView out, int64_t* d_count, cudaStream_t st);
+
+// Apply a primitive op list to every term (QuantumState::apply_* loops).
+cudaError_t launch_apply_ops(const uint32_t* d_ops, int nops, TermsView terms, int* status,
+                             cudaStream_t st);
+
+// Project every term on (qubit, outcome): keep[i] = 0 if impossible; the
+// coefficient is amplified by -1 for random outcomes (projection.rs:27-57).
+cudaError_t launch_project(TermsView terms, int qubit, int outcome, int32_t* keep, int* status,
+                           cudaStream_t st);
+
+// Discard qubit from every term (n -> n-1, same W storage).
+cudaError_t launch_discard(TermsView terms, int qubit, int* status, cudaStream_t st);
+
+// Unpack to bool bytes (the nsg_export_terms layout) / pack from them.
+cudaError_t launch_unpack(const TermsView& t, uint8_t* G, uint8_t* F, uint8_t* M, uint8_t* gam,
+                          uint8_t* v, uint8_t* s, cudaStream_t st);
+cudaError_t launch_pack(TermsView t, const uint8_t* G, const uint8_t* F, const uint8_t* M,
+                        const uint8_t* gam, const uint8_t* v, const uint8_t* s, cudaStream_t st);
+
+// Bra frames (U_C^{-1} tableau) of every term; n ≤ 64.
+cudaError_t launch_frames(const TermsView& t, FrameView fr, cudaStream_t st);
+
+// Pauli frames: x_{A,P} and Z8 phase k_{A,P} for every (term A, observable P).
+cudaError_t launch_pauli_frames(const TermsView& t, const DevPauli* d_paulis, int nobs,
+                                uint64_t* x_out, uint8_t* k_out, cudaStream_t st);
+
+struct PairLaunch {
+    TermsView A;   // bra terms (frames computed from these)
+    FrameView fr;  // frames of A
+    TermsView B;   // ket terms
+    const uint64_t* px = nullptr;  // [chiA][nobs] x_{A,P}
+    const uint8_t* pk = nullptr;   // [chiA][nobs] k_{A,P}
+    int nobs = 1;
+    bool triangular = true;  // exp_value/norm (A == B, i ≤ j) vs inner product (all pairs)
+    bool complex_out = false;
+    bool mixed = false;
+    int chunk = 32;
+    int64_t total_chunks = 0;
+    const int64_t* row_chunk_off = nullptr;  // triangular: [chiA+1] prefix of chunks per row
+    double* partials = nullptr;              // [nwarps][nobs][8]
+    int nwarps = 0;
+    int blocks = 0;
+    int warps_per_block = 4;
+    int* status = nullptr;
+    uint8_t* dbg_k = nullptr;   // optional per-pair dump [chiA][chiB]
+    int32_t* dbg_r = nullptr;
+};
+
+cudaError_t launch_pairs(const PairLaunch& p, cudaStream_t st);
+
+// Reduce per-warp partials to one value (re, im) per observable, scaled by
+// `scale` (|global factor|² or the complex conj(g_a)·g_b).
+cudaError_t launch_reduce(const double* partials, int nwarps, int nobs, bool complex_out,
+                          double scale_re, double scale_im, double* out, cudaStream_t st);
+
+// Dense statevector of the decomposed state (n ≤ 28): out[2^n] complex.
+cudaError_t launch_statevector(const TermsView& t, double gf_re, double gf_im, double* out,
+                               cudaStream_t st);
+
+int device_sm_count();
+
+// Integer-pipe probe kernel (measurement helper).
+cudaError_t launch_int_probe(uint64_t iters, int blocks, int threads, uint32_t* sink, cudaStream_t st);
+
+}  // namespace nsg

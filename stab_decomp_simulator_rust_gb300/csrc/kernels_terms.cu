@@ -1,0 +1,527 @@
+// kernels_terms.cu — per-term kernels: compile (kron + Clifford run +
+// post-selection + discard), stable compaction, gate application, projection,
+// discard, pack/unpack and the dense statevector.
+//
+// One warp owns one term (warp_chform.cuh); a block of 4 warps stages the
+// shared primitive-op list through shared memory so all warps of the block
+// read each op from one broadcast load.
+#include <cuda_runtime.h>
+
+#include "device_state.hpp"
+#include "warp_chform.cuh"
+
+namespace nsg {
+namespace {
+
+using dev::BV;
+using dev::WarpCH;
+
+constexpr int WARPS = 4;
+constexpr int OPS_CHUNK = 2048;
+
+template <int W>
+using Eng = WarpCH<uint64_t, W, 2 * W>;
+
+// ---- load / store a term between HBM (any storage W) and a warp engine -----
+template <int W>
+__device__ __forceinline__ void load_term(Eng<W>& e, const TermsView& tv, int64_t term) {
+    e.n = tv.n;
+    e.err = 0;
+    e.phase = tv.phase[term];
+    e.gam = 0;
+#pragma unroll
+    for (int k = 0; k < 2 * W; k++) {
+        int r = 32 * k + e.lane;
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            uint64_t g = 0, f = 0, m = 0;
+            if (r < tv.R && w < tv.W) {
+                size_t idx = ((size_t)term * tv.R + r) * tv.W + w;
+                g = tv.G[idx];
+                f = tv.F[idx];
+                m = tv.M[idx];
+            }
+            e.G[k].w[w] = g;
+            e.F[k].w[w] = f;
+            e.M[k].w[w] = m;
+        }
+        int gw = r >> 6;
+        uint64_t gl = (gw < tv.W) ? tv.GL[(size_t)term * tv.W + gw] : 0;
+        uint64_t gh = (gw < tv.W) ? tv.GH[(size_t)term * tv.W + gw] : 0;
+        int g = (int)((gl >> (r & 63)) & 1) | ((int)((gh >> (r & 63)) & 1) << 1);
+        e.gam_set(k, g);
+    }
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        e.v.w[w] = (w < tv.W) ? tv.V[(size_t)term * tv.W + w] : 0;
+        e.s.w[w] = (w < tv.W) ? tv.S[(size_t)term * tv.W + w] : 0;
+    }
+}
+
+template <int W>
+__device__ __forceinline__ void store_term(const Eng<W>& e, const TermsView& tv, int64_t term) {
+#pragma unroll
+    for (int k = 0; k < 2 * W; k++) {
+        int r = 32 * k + e.lane;
+        if (r < tv.R) {
+#pragma unroll
+            for (int w = 0; w < 2; w++) {
+                if (w < tv.W) {
+                    size_t idx = ((size_t)term * tv.R + r) * tv.W + w;
+                    tv.G[idx] = (w < W) ? e.G[k].w[(w < W) ? w : 0] : 0;
+                    tv.F[idx] = (w < W) ? e.F[k].w[(w < W) ? w : 0] : 0;
+                    tv.M[idx] = (w < W) ? e.M[k].w[(w < W) ? w : 0] : 0;
+                }
+            }
+        }
+    }
+    // γ planes by ballot: slot k covers rows 32k..32k+31 = word k/2, half k%2.
+    uint64_t gl[2] = {0, 0}, gh[2] = {0, 0};
+#pragma unroll
+    for (int k = 0; k < 2 * W; k++) {
+        int g = e.gam_of(k);
+        uint32_t b0 = __ballot_sync(dev::FULL, g & 1);
+        uint32_t b1 = __ballot_sync(dev::FULL, (g >> 1) & 1);
+        gl[k >> 1] |= (uint64_t)b0 << (32 * (k & 1));
+        gh[k >> 1] |= (uint64_t)b1 << (32 * (k & 1));
+    }
+    if (e.lane == 0) {
+#pragma unroll
+        for (int w = 0; w < 2; w++) {
+            if (w < tv.W) {
+                tv.GL[(size_t)term * tv.W + w] = gl[w];
+                tv.GH[(size_t)term * tv.W + w] = gh[w];
+                tv.V[(size_t)term * tv.W + w] = (w < W) ? e.v.w[(w < W) ? w : 0] : 0;
+                tv.S[(size_t)term * tv.W + w] = (w < W) ? e.s.w[(w < W) ? w : 0] : 0;
+            }
+        }
+        tv.phase[term] = (uint8_t)e.phase;
+    }
+}
+
+template <int W>
+__device__ __forceinline__ void apply_prim(Eng<W>& e, uint32_t code) {
+    uint32_t op = code & 0xff, a = (code >> 8) & 0xff, b = (code >> 16) & 0xff;
+    switch (op) {
+        case P_H: e.left_h(a); break;
+        case P_X: e.left_x(a); break;
+        case P_Y: e.left_y(a); break;
+        case P_Z: e.left_z(a); break;
+        case P_S: e.left_s(a); break;
+        case P_SDG: e.left_sdg(a); break;
+        case P_CX: e.left_cx(a, b); break;
+        case P_CZ: e.left_cz(a, b); break;
+        default: e.err = 9; break;
+    }
+}
+
+// ---- compile ------------------------------------------------------------------
+template <int W>
+__global__ void __launch_bounds__(WARPS * 32) compile_kernel(
+    const uint32_t* __restrict__ ops, int nops, int n, int t, int64_t chi_t,
+    const uint64_t* __restrict__ tG, const uint64_t* __restrict__ tF, const uint64_t* __restrict__ tM,
+    const uint8_t* __restrict__ tGam, const uint64_t* __restrict__ tV, const uint64_t* __restrict__ tS,
+    const uint8_t* __restrict__ tPhase, const uint8_t* __restrict__ tCk, const int32_t* __restrict__ tCr,
+    TermsView out, int32_t* __restrict__ keep, int* __restrict__ status) {
+    __shared__ uint32_t sops[OPS_CHUNK];
+    const int lane = threadIdx.x & 31;
+    const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    const bool active = term < chi_t;
+    const int width = n + t;
+
+    Eng<W> e;
+    e.lane = lane;
+    e.init_zero(width);
+    if (active) {
+        // kron(|0^n⟩, T-term) (form/kron.rs:12-59): T rows shifted by n rows and n columns.
+#pragma unroll
+        for (int k = 0; k < 2 * W; k++) {
+            int r = 32 * k + lane;
+            if (r >= n && r < width) {
+                int tr = r - n;
+                size_t idx = (size_t)term * t + tr;
+                BV<uint64_t, W> g = BV<uint64_t, W>::zero(), f = g, m = g;
+                uint64_t gw = tG[idx], fw = tF[idx], mw = tM[idx];
+#pragma unroll
+                for (int w = 0; w < W; w++) {
+                    int lo = 64 * w;
+                    // bit c of the shifted row = bit (c - n) of the T row
+                    auto sh = [&](uint64_t x) -> uint64_t {
+                        int off = lo - n;  // T bit index of this word's bit 0
+                        if (off >= 64 || off <= -64) return 0;
+                        return off >= 0 ? (x >> off) : (x << (-off));
+                    };
+                    g.w[w] = sh(gw);
+                    f.w[w] = sh(fw);
+                    m.w[w] = sh(mw);
+                }
+                e.G[k] = g;
+                e.F[k] = f;
+                e.M[k] = m;
+                e.gam_set(k, tGam[idx]);
+            }
+        }
+        uint64_t vv = tV[term], ss = tS[term];
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            int off = 64 * w - n;
+            e.v.w[w] = (off >= 64 || off <= -64) ? 0 : (off >= 0 ? (vv >> off) : (vv << (-off)));
+            e.s.w[w] = (off >= 64 || off <= -64) ? 0 : (off >= 0 ? (ss >> off) : (ss << (-off)));
+        }
+        e.phase = tPhase[term];
+    }
+
+    for (int base = 0; base < nops; base += OPS_CHUNK) {
+        int cnt = min(OPS_CHUNK, nops - base);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) sops[i] = ops[base + i];
+        __syncthreads();
+        if (active && !e.err) {
+            for (int i = 0; i < cnt; i++) apply_prim<W>(e, sops[i]);
+        }
+    }
+    if (!active) return;
+
+    // Post-select the ancillas onto |0⟩ in reverse order (compiler/mod.rs:104-120).
+    int ndet = 0;
+    bool ok = true;
+    for (int q = width - 1; q >= n && !e.err; q--) {
+        int r = e.project(q, false);
+        if (r < 0) {
+            ok = false;
+            break;
+        }
+        ndet += r;
+    }
+    if (ok && !e.err) {
+        for (int q = width - 1; q >= n && !e.err; q--) e.discard(q);  // :124-127
+    }
+    if (e.err) {
+        if (lane == 0) atomicOr(status, e.err == 2 ? DS_CANNOT_DISCARD : DS_INVARIANT);
+        ok = false;
+    }
+    if (lane == 0) {
+        keep[term] = ok ? 1 : 0;
+        out.coef_k[term] = tCk[term];
+        out.coef_r[term] = tCr[term] - ndet;  // coeff.amplify(ndet) (scalar.rs:108-119)
+    }
+    if (ok) store_term<W>(e, out, term);
+}
+
+// ---- compaction -------------------------------------------------------------
+__global__ void scan_keep_kernel(const int32_t* __restrict__ keep, int64_t n, int32_t* __restrict__ pos,
+                                 int64_t* __restrict__ count) {
+    // Single block exclusive scan (χ ≤ a few 10^6).
+    __shared__ int32_t warp_tot[32];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int64_t base = 0; base < n; base += blockDim.x) {
+        int64_t i = base + threadIdx.x;
+        int32_t x = (i < n) ? keep[i] : 0;
+        int32_t incl = x;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            int32_t y = __shfl_up_sync(dev::FULL, incl, d);
+            if (lane >= d) incl += y;
+        }
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            int32_t w = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : 0;
+            int32_t wi = w;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                int32_t y = __shfl_up_sync(dev::FULL, wi, d);
+                if (lane >= d) wi += y;
+            }
+            warp_tot[lane] = wi - w;  // exclusive
+        }
+        __syncthreads();
+        int64_t excl = carry + warp_tot[wid] + incl - x;
+        if (i < n) pos[i] = (int32_t)excl;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry = excl + x;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count = carry;
+}
+
+__global__ void gather_kernel(TermsView in, const int32_t* __restrict__ keep, const int32_t* __restrict__ pos,
+                              TermsView out) {
+    const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (term >= in.chi || !keep[term]) return;
+    const int64_t dst = pos[term];
+    const size_t rowwords = (size_t)in.R * in.W;
+    for (size_t i = lane; i < rowwords; i += 32) {
+        out.G[dst * rowwords + i] = in.G[term * rowwords + i];
+        out.F[dst * rowwords + i] = in.F[term * rowwords + i];
+        out.M[dst * rowwords + i] = in.M[term * rowwords + i];
+    }
+    for (int w = lane; w < in.W; w += 32) {
+        out.V[dst * in.W + w] = in.V[term * in.W + w];
+        out.S[dst * in.W + w] = in.S[term * in.W + w];
+        out.GL[dst * in.W + w] = in.GL[term * in.W + w];
+        out.GH[dst * in.W + w] = in.GH[term * in.W + w];
+    }
+    if (lane == 0) {
+        out.phase[dst] = in.phase[term];
+        out.coef_k[dst] = in.coef_k[term];
+        out.coef_r[dst] = in.coef_r[term];
+    }
+}
+
+// ---- gate application / projection / discard on a compiled state ----------
+template <int W>
+__global__ void __launch_bounds__(WARPS * 32) apply_ops_kernel(const uint32_t* __restrict__ ops, int nops,
+                                                              TermsView tv, int* __restrict__ status) {
+    __shared__ uint32_t sops[OPS_CHUNK];
+    const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    const bool active = term < tv.chi;
+    Eng<W> e;
+    e.lane = threadIdx.x & 31;
+    if (active) load_term<W>(e, tv, term);
+    for (int base = 0; base < nops; base += OPS_CHUNK) {
+        int cnt = min(OPS_CHUNK, nops - base);
+        __syncthreads();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) sops[i] = ops[base + i];
+        __syncthreads();
+        if (active && !e.err)
+            for (int i = 0; i < cnt; i++) apply_prim<W>(e, sops[i]);
+    }
+    if (!active) return;
+    if (e.err && e.lane == 0) atomicOr(status, DS_INVARIANT);
+    store_term<W>(e, tv, term);
+}
+
+template <int W>
+__global__ void __launch_bounds__(WARPS * 32) project_kernel(TermsView tv, int q, int outcome,
+                                                            int32_t* __restrict__ keep, int* __restrict__ status) {
+    const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    if (term >= tv.chi) return;
+    Eng<W> e;
+    e.lane = threadIdx.x & 31;
+    load_term<W>(e, tv, term);
+    int r = e.project(q, outcome != 0);
+    if (e.err) {
+        if (e.lane == 0) atomicOr(status, DS_INVARIANT);
+        r = -1;
+    }
+    if (e.lane == 0) {
+        keep[term] = (r >= 0) ? 1 : 0;
+        if (r == 0) tv.coef_r[term] += 1;  // amplify(-1): r -= -1 (projection.rs:44)
+    }
+    if (r == 0) store_term<W>(e, tv, term);
+}
+
+template <int W>
+__global__ void __launch_bounds__(WARPS * 32) discard_kernel(TermsView tv, int q, int* __restrict__ status) {
+    const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    if (term >= tv.chi) return;
+    Eng<W> e;
+    e.lane = threadIdx.x & 31;
+    load_term<W>(e, tv, term);
+    e.discard(q);
+    if (e.err && e.lane == 0) atomicOr(status, e.err == 2 ? DS_CANNOT_DISCARD : DS_INVARIANT);
+    store_term<W>(e, tv, term);  // width n-1 in the same storage
+}
+
+// ---- pack / unpack bool bytes -------------------------------------------------
+__global__ void unpack_kernel(TermsView tv, uint8_t* G, uint8_t* F, uint8_t* M, uint8_t* gam, uint8_t* v,
+                              uint8_t* s) {
+    const int n = tv.n;
+    const int64_t total = tv.chi * n * n;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t term = i / ((int64_t)n * n);
+        int rc = (int)(i % ((int64_t)n * n));
+        int r = rc / n, c = rc % n;
+        size_t idx = ((size_t)term * tv.R + r) * tv.W + (c >> 6);
+        G[i] = (tv.G[idx] >> (c & 63)) & 1;
+        F[i] = (tv.F[idx] >> (c & 63)) & 1;
+        M[i] = (tv.M[idx] >> (c & 63)) & 1;
+        if (c == 0) {
+            size_t w = (size_t)term * tv.W + (r >> 6);
+            int g = (int)((tv.GL[w] >> (r & 63)) & 1) | ((int)((tv.GH[w] >> (r & 63)) & 1) << 1);
+            gam[term * n + r] = (uint8_t)(2 * g);  // Z8 exponent of the reference's PhaseFactor
+            v[term * n + r] = (tv.V[w] >> (r & 63)) & 1;
+            s[term * n + r] = (tv.S[w] >> (r & 63)) & 1;
+        }
+    }
+}
+
+__global__ void pack_kernel(TermsView tv, const uint8_t* G, const uint8_t* F, const uint8_t* M, const uint8_t* gam,
+                            const uint8_t* v, const uint8_t* s) {
+    // one thread per (term, row word): builds the words of row r
+    const int n = tv.n;
+    const int64_t total = tv.chi * tv.R;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        int64_t term = i / tv.R;
+        int r = (int)(i % tv.R);
+        for (int w = 0; w < tv.W; w++) {
+            uint64_t g = 0, f = 0, m = 0;
+            if (r < n) {
+                for (int b = 0; b < 64; b++) {
+                    int c = 64 * w + b;
+                    if (c >= n) break;
+                    size_t bi = ((size_t)term * n + r) * n + c;
+                    g |= (uint64_t)(G[bi] & 1) << b;
+                    f |= (uint64_t)(F[bi] & 1) << b;
+                    m |= (uint64_t)(M[bi] & 1) << b;
+                }
+            }
+            size_t idx = ((size_t)term * tv.R + r) * tv.W + w;
+            tv.G[idx] = g;
+            tv.F[idx] = f;
+            tv.M[idx] = m;
+        }
+        if (r < tv.W) {  // vectors: thread r of the term builds word r
+            int w = r;
+            uint64_t gl = 0, gh = 0, vv = 0, ss = 0;
+            for (int b = 0; b < 64; b++) {
+                int q = 64 * w + b;
+                if (q >= n) break;
+                int g = (gam[term * n + q] >> 1) & 3;
+                gl |= (uint64_t)(g & 1) << b;
+                gh |= (uint64_t)((g >> 1) & 1) << b;
+                vv |= (uint64_t)(v[term * n + q] & 1) << b;
+                ss |= (uint64_t)(s[term * n + q] & 1) << b;
+            }
+            tv.GL[term * tv.W + w] = gl;
+            tv.GH[term * tv.W + w] = gh;
+            tv.V[term * tv.W + w] = vv;
+            tv.S[term * tv.W + w] = ss;
+        }
+    }
+}
+
+// ---- dense statevector (n ≤ 28; tests and to_statevector) -------------------
+// ⟨x|U_C U_H|s⟩ = i^{Σ_{p∈x}γ_p}·(-1)^{Σ_{p<q∈x} M_p·F_q + u·m + Σ_{j∈v} u_j s_j}·2^{-|v|/2}
+// with u = xF, m = xM, nonzero iff u_j = s_j for all j ∉ v.  Same value as
+// amplitude_at_computational_basis (form/amplitude.rs:28-44).
+__global__ void statevector_kernel(TermsView tv, double gf_re, double gf_im, double* __restrict__ out) {
+    const int n = tv.n;
+    const int64_t dim = (int64_t)1 << n;
+    const double r2 = 0.70710678118654752440;
+    const double cr[8] = {1, r2, 0, -r2, -1, -r2, 0, r2};
+    const double ci[8] = {0, r2, 1, r2, 0, -r2, -1, -r2};
+    for (int64_t x = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; x < dim; x += (int64_t)gridDim.x * blockDim.x) {
+        double ar = 0.0, ai = 0.0;
+        for (int64_t term = 0; term < tv.chi; term++) {
+            const uint64_t* F = tv.F + (size_t)term * tv.R * tv.W;
+            const uint64_t* M = tv.M + (size_t)term * tv.R * tv.W;
+            uint64_t u = 0, m = 0;
+            int cnt = 0, gsum = 0;
+            uint64_t gl = tv.GL[term * tv.W], gh = tv.GH[term * tv.W];
+            for (int p = 0; p < n; p++) {
+                if ((x >> p) & 1) {
+                    uint64_t fp = F[(size_t)p * tv.W], mp = M[(size_t)p * tv.W];
+                    cnt += __popcll(m & fp);
+                    u ^= fp;
+                    m ^= mp;
+                    gsum += (int)((gl >> p) & 1) + 2 * (int)((gh >> p) & 1);
+                }
+            }
+            uint64_t v = tv.V[term * tv.W], s = tv.S[term * tv.W];
+            if (((u ^ s) & ~v) != 0) continue;
+            cnt += __popcll(u & m) + __popcll(u & v & s);
+            int k = (tv.phase[term] + 2 * gsum + 4 * (cnt & 1) + tv.coef_k[term]) & 7;
+            int rr = __popcll(v) + tv.coef_r[term];
+            double mag = exp2(-0.5 * (double)rr);
+            ar += mag * cr[k];
+            ai += mag * ci[k];
+        }
+        out[2 * x] = ar * gf_re - ai * gf_im;
+        out[2 * x + 1] = ar * gf_im + ai * gf_re;
+    }
+}
+
+inline int blocks_for(int64_t chi) { return (int)((chi + WARPS - 1) / WARPS); }
+
+}  // namespace
+
+cudaError_t launch_compile(const uint32_t* d_ops, int nops, int n, int t, int64_t chi_t, const uint64_t* tG,
+                           const uint64_t* tF, const uint64_t* tM, const uint8_t* tGam, const uint64_t* tV,
+                           const uint64_t* tS, const uint8_t* tPhase, const uint8_t* tCk, const int32_t* tCr,
+                           TermsView out, int32_t* keep, int* status, cudaStream_t st) {
+    if (chi_t == 0) return cudaSuccess;
+    int width = n + t;
+    dim3 grid(blocks_for(chi_t)), block(WARPS * 32);
+    if (width <= 64)
+        compile_kernel<1><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase, tCk,
+                                                  tCr, out, keep, status);
+    else
+        compile_kernel<2><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase, tCk,
+                                                  tCr, out, keep, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_compact(const TermsView& in, const int32_t* keep, int32_t* scan_tmp, TermsView out,
+                           int64_t* d_count, cudaStream_t st) {
+    if (in.chi == 0) return cudaMemsetAsync(d_count, 0, sizeof(int64_t), st);
+    scan_keep_kernel<<<1, 1024, 0, st>>>(keep, in.chi, scan_tmp, d_count);
+    gather_kernel<<<blocks_for(in.chi), WARPS * 32, 0, st>>>(in, keep, scan_tmp, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_apply_ops(const uint32_t* d_ops, int nops, TermsView terms, int* status, cudaStream_t st) {
+    if (terms.chi == 0 || nops == 0) return cudaSuccess;
+    if (terms.W == 1)
+        apply_ops_kernel<1><<<blocks_for(terms.chi), WARPS * 32, 0, st>>>(d_ops, nops, terms, status);
+    else
+        apply_ops_kernel<2><<<blocks_for(terms.chi), WARPS * 32, 0, st>>>(d_ops, nops, terms, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project(TermsView terms, int qubit, int outcome, int32_t* keep, int* status, cudaStream_t st) {
+    if (terms.chi == 0) return cudaSuccess;
+    if (terms.W == 1)
+        project_kernel<1><<<blocks_for(terms.chi), WARPS * 32, 0, st>>>(terms, qubit, outcome, keep, status);
+    else
+        project_kernel<2><<<blocks_for(terms.chi), WARPS * 32, 0, st>>>(terms, qubit, outcome, keep, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_discard(TermsView terms, int qubit, int* status, cudaStream_t st) {
+    if (terms.chi == 0) return cudaSuccess;
+    if (terms.W == 1)
+        discard_kernel<1><<<blocks_for(terms.chi), WARPS * 32, 0, st>>>(terms, qubit, status);
+    else
+        discard_kernel<2><<<blocks_for(terms.chi), WARPS * 32, 0, st>>>(terms, qubit, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const TermsView& t, uint8_t* G, uint8_t* F, uint8_t* M, uint8_t* gam, uint8_t* v,
+                          uint8_t* s, cudaStream_t st) {
+    if (t.chi == 0) return cudaSuccess;
+    int64_t total = t.chi * t.n * t.n;
+    int blocks = (int)std::min<int64_t>((total + 255) / 256, 65535);
+    unpack_kernel<<<blocks, 256, 0, st>>>(t, G, F, M, gam, v, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack(TermsView t, const uint8_t* G, const uint8_t* F, const uint8_t* M, const uint8_t* gam,
+                        const uint8_t* v, const uint8_t* s, cudaStream_t st) {
+    if (t.chi == 0) return cudaSuccess;
+    int64_t total = t.chi * t.R;
+    int blocks = (int)std::min<int64_t>((total + 255) / 256, 65535);
+    pack_kernel<<<blocks, 256, 0, st>>>(t, G, F, M, gam, v, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_statevector(const TermsView& t, double gf_re, double gf_im, double* out, cudaStream_t st) {
+    int64_t dim = (int64_t)1 << t.n;
+    int blocks = (int)std::min<int64_t>((dim + 255) / 256, 65535);
+    statevector_kernel<<<blocks, 256, 0, st>>>(t, gf_re, gf_im, out);
+    return cudaGetLastError();
+}
+
+int device_sm_count() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return sms > 0 ? sms : 1;
+}
+
+}  // namespace nsg

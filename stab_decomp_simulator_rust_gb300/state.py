@@ -1,0 +1,239 @@
+"""QuantumState — the compiled stabilizer decomposition, resident on the GPU.
+
+Method names, arguments and errors mirror the reference's Python class
+(python/necstar/state.pyi:9-379 over python/src/state.rs:13-222): every
+failure raises ValueError (here NecstarError, a ValueError subclass carrying
+the status code).  All work runs in libnecstar_gpu.so; the batched form
+``exp_values`` evaluates many observables in one pass over the χ² pairs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _ffi
+from ._ffi import check
+from .circuit import QuantumCircuit, QuantumGate, gate_rows
+from .pauli import PauliString
+
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+
+
+def seed_bytes(seed) -> np.ndarray | None:
+    """Python seed → 32 bytes (python/src/utils.rs:4-39)."""
+    if seed is None:
+        return None
+    if isinstance(seed, (bytes, bytearray)):
+        if len(seed) != 32:
+            raise ValueError(f"Seed must be 32 bytes, got {len(seed)}")
+        return np.frombuffer(bytes(seed), dtype=np.uint8).copy()
+    if isinstance(seed, int):
+        if 0 <= seed < (1 << 64):
+            b = seed.to_bytes(8, "little") + bytes(24)
+        else:
+            b = seed.to_bytes(32, "little")
+        return np.frombuffer(b, dtype=np.uint8).copy()
+    raise TypeError("Seed must be an integer or 32 bytes")
+
+
+def _p(a: np.ndarray | None):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class QuantumState:
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _ffi.load().nsg_state_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    # ---- construction
+    @staticmethod
+    def from_circuit(circuit: QuantumCircuit) -> "QuantumState":
+        return QuantumState.from_gates(circuit.num_qubits, circuit.gate_array())
+
+    @staticmethod
+    def from_gates(num_qubits: int, gates) -> "QuantumState":
+        L = _ffi.load()
+        rows = gate_rows(gates)
+        h = C.c_void_p()
+        check(L.nsg_state_from_circuit(num_qubits, _p(rows), len(rows), C.byref(h)))
+        return QuantumState(h)
+
+    @staticmethod
+    def from_terms(d: dict) -> "QuantumState":
+        """Build from a term dump (the layout of ``export_terms``)."""
+        L = _ffi.load()
+        n = int(d["n"])
+        chi = int(len(d["phase"]))
+        u8 = lambda k: np.ascontiguousarray(d[k], dtype=np.uint8)
+        arrs = [u8(k) for k in ("G", "F", "M", "gamma", "v", "s", "phase", "coef_phase")]
+        r = np.ascontiguousarray(d["coef_r"], dtype=np.int32)
+        z = np.ascontiguousarray(d.get("coef_zero", np.zeros(chi)), dtype=np.uint8)
+        gf = np.ascontiguousarray(d.get("global_factor", [1.0, 0.0]), dtype=np.float64)
+        h = C.c_void_p()
+        check(L.nsg_state_from_terms(n, chi, *[_p(a) for a in arrs], _p(r), _p(z), _p(gf), C.byref(h)))
+        return QuantumState(h)
+
+    def clone(self) -> "QuantumState":
+        h = C.c_void_p()
+        check(_ffi.load().nsg_state_clone(self._h, C.byref(h)))
+        return QuantumState(h)
+
+    def set_stream(self, cuda_stream: int | None) -> None:
+        """Run this state's work on a caller-owned cudaStream_t (an integer handle)."""
+        check(_ffi.load().nsg_state_set_stream(self._h, C.c_void_p(cuda_stream or 0)))
+
+    # ---- properties
+    @property
+    def num_qubits(self) -> int:
+        v = C.c_uint32()
+        check(_ffi.load().nsg_num_qubits(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def stabilizer_rank(self) -> int:
+        v = C.c_uint64()
+        check(_ffi.load().nsg_stabilizer_rank(self._h, C.byref(v)))
+        return v.value
+
+    def __str__(self) -> str:
+        return f"QuantumState(num_qubits={self.num_qubits}, stabilizer_rank={self.stabilizer_rank})"
+
+    # ---- pair sums
+    def exp_value(self, pauli_string: PauliString) -> float:
+        out = C.c_double()
+        a = pauli_string.abi()
+        check(_ffi.load().nsg_exp_value(self._h, C.byref(a), C.byref(out)))
+        return out.value
+
+    def exp_values(self, paulis, precision: int = PRECISION_FP64) -> np.ndarray:
+        """Batched expectation values: one pass over the pairs for all observables."""
+        paulis = list(paulis)
+        arr = (_ffi.PauliABI * max(len(paulis), 1))()
+        for i, p in enumerate(paulis):
+            arr[i] = p.abi()
+        out = np.zeros(len(paulis), np.float64)
+        check(_ffi.load().nsg_exp_value_batch(self._h, arr, len(paulis), precision, _p(out)))
+        return out
+
+    def inner_product(self, other: "QuantumState") -> complex:
+        out = np.zeros(2, np.float64)
+        check(_ffi.load().nsg_inner_product(self._h, other._h, _p(out)))
+        return complex(out[0], out[1])
+
+    def norm(self) -> float:
+        out = C.c_double()
+        check(_ffi.load().nsg_norm(self._h, C.byref(out)))
+        return out.value
+
+    # ---- projection / measurement
+    def project_normalized(self, qubit: int, outcome: bool) -> None:
+        check(_ffi.load().nsg_project_normalized(self._h, qubit, int(bool(outcome))))
+
+    def project_unnormalized(self, qubit: int, outcome: bool) -> None:
+        check(_ffi.load().nsg_project_unnormalized(self._h, qubit, int(bool(outcome))))
+
+    def discard(self, qubit: int) -> None:
+        check(_ffi.load().nsg_discard(self._h, qubit))
+
+    def measure(self, qargs, seed=None) -> list[bool]:
+        q = np.ascontiguousarray(list(qargs), dtype=np.uint32)
+        out = np.zeros(max(len(q), 1), np.uint8)
+        check(_ffi.load().nsg_measure(self._h, _p(q), len(q), _p(seed_bytes(seed)), _p(out)))
+        return [bool(x) for x in out[:len(q)]]
+
+    def measure_all(self, seed=None) -> list[bool]:
+        n = self.num_qubits
+        out = np.zeros(max(n, 1), np.uint8)
+        check(_ffi.load().nsg_measure_all(self._h, _p(seed_bytes(seed)), _p(out)))
+        return [bool(x) for x in out[:n]]
+
+    def sample_raw(self, qargs, shots: int, seed=None):
+        """Returns (outcomes as Python ints with bit i ↔ qargs[i], counts)."""
+        L = _ffi.load()
+        q = np.ascontiguousarray(list(qargs), dtype=np.uint32)
+        cap = int(min(max(shots, 1), 1 << 20))
+        while True:
+            outc = np.zeros(2 * cap, np.uint64)
+            cnts = np.zeros(cap, np.uint64)
+            nout = C.c_size_t()
+            rc = L.nsg_sample(self._h, _p(q), len(q), shots, _p(seed_bytes(seed)), _p(outc), _p(cnts), cap,
+                              C.byref(nout))
+            if rc == 104 and nout.value > cap:  # NSG_ERR_BUFFER_TOO_SMALL
+                cap = nout.value
+                continue
+            check(rc)
+            k = nout.value
+            vals = [int(outc[2 * i]) | (int(outc[2 * i + 1]) << 64) for i in range(k)]
+            return vals, [int(c) for c in cnts[:k]]
+
+    def sample(self, qargs, shots: int, seed=None) -> dict[str, int]:
+        """Counts keyed by outcome strings: character i is qargs[i] (python/src/state.rs:64-90)."""
+        qargs = list(qargs)
+        vals, cnts = self.sample_raw(qargs, shots, seed)
+        k = len(qargs)
+        return {"".join("1" if (v >> i) & 1 else "0" for i in range(k)): c for v, c in zip(vals, cnts)}
+
+    # ---- gates
+    def apply_gate(self, gate: QuantumGate) -> None:
+        self.apply_gates([gate])
+
+    def apply_gates(self, gates) -> None:
+        rows = gate_rows(gates)
+        check(_ffi.load().nsg_apply_gates(self._h, _p(rows), len(rows)))
+
+    def apply_x(self, q): self.apply_gate(QuantumGate.x(q))
+    def apply_y(self, q): self.apply_gate(QuantumGate.y(q))
+    def apply_z(self, q): self.apply_gate(QuantumGate.z(q))
+    def apply_h(self, q): self.apply_gate(QuantumGate.h(q))
+    def apply_s(self, q): self.apply_gate(QuantumGate.s(q))
+    def apply_sdg(self, q): self.apply_gate(QuantumGate.sdg(q))
+    def apply_sqrt_x(self, q): self.apply_gate(QuantumGate.sqrt_x(q))
+    def apply_sqrt_xdg(self, q): self.apply_gate(QuantumGate.sqrt_xdg(q))
+    def apply_cx(self, c, t): self.apply_gate(QuantumGate.cx(c, t))
+    def apply_cz(self, a, b): self.apply_gate(QuantumGate.cz(a, b))
+    def apply_swap(self, a, b): self.apply_gate(QuantumGate.swap(a, b))
+
+    def debug_pair_values(self, pauli: PauliString | None = None):
+        """Exact ⟨S_i|P|S_j⟩ for all pairs: (k, r) arrays of shape (χ, χ); k = 255 means 0."""
+        chi = self.stabilizer_rank
+        k = np.zeros((chi, chi), np.uint8)
+        r = np.zeros((chi, chi), np.int32)
+        if pauli is None:
+            check(_ffi.load().nsg_debug_pair_values(self._h, None, _p(k), _p(r)))
+        else:
+            a = pauli.abi()
+            check(_ffi.load().nsg_debug_pair_values(self._h, C.byref(a), _p(k), _p(r)))
+        return k, r
+
+    # ---- dense views (tests)
+    def to_statevector(self) -> np.ndarray:
+        n = self.num_qubits
+        out = np.zeros(2 << n if n < 28 else 2, np.float64)
+        check(_ffi.load().nsg_to_statevector(self._h, _p(out), 1 << n if n < 28 else 1))
+        return out[0::2] + 1j * out[1::2]
+
+    def export_terms(self) -> dict:
+        """Every term as bool bytes (the parity-dump / checkpoint format)."""
+        n, chi = self.num_qubits, self.stabilizer_rank
+        d = {
+            "n": n,
+            "G": np.zeros((chi, n, n), np.uint8), "F": np.zeros((chi, n, n), np.uint8),
+            "M": np.zeros((chi, n, n), np.uint8), "gamma": np.zeros((chi, n), np.uint8),
+            "v": np.zeros((chi, n), np.uint8), "s": np.zeros((chi, n), np.uint8),
+            "phase": np.zeros(chi, np.uint8), "coef_phase": np.zeros(chi, np.uint8),
+            "coef_r": np.zeros(chi, np.int32), "coef_zero": np.zeros(chi, np.uint8),
+            "global_factor": np.zeros(2, np.float64),
+        }
+        keys = ("G", "F", "M", "gamma", "v", "s", "phase", "coef_phase", "coef_r", "coef_zero", "global_factor")
+        check(_ffi.load().nsg_export_terms(self._h, *[_p(d[k]) for k in keys]))
+        return d
