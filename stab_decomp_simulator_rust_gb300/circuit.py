@@ -25,11 +25,15 @@ _ALIASES = {"h": "H", "x": "X", "y": "Y", "z": "Z", "s": "S", "sdg": "SDG", "sx"
 class QuantumGate:
     """One gate: opcode and qubits (QuantumGate, crates/necstar/src/circuit/gates.rs:7-42)."""
 
-    __slots__ = ("op", "qubits")
+    __slots__ = ("op", "_q")
 
     def __init__(self, op: int, qubits):
         self.op = int(op)
-        self.qubits = tuple(int(q) for q in qubits)
+        self._q = tuple(int(q) for q in qubits)
+
+    @property
+    def qubits(self) -> list[int]:
+        return list(self._q)
 
     @property
     def name(self) -> str:
@@ -38,18 +42,23 @@ class QuantumGate:
     def is_clifford(self) -> bool:
         return self.op <= OP["SWAP"]
 
-    def is_t_type_gate(self) -> bool:
+    def is_t_type(self) -> bool:
         return self.op in (OP["T"], OP["TDG"])
 
+    is_t_type_gate = is_t_type
+
     def row(self) -> tuple[int, int, int, int]:
-        q = list(self.qubits) + [0, 0, 0]
+        q = list(self._q) + [0, 0, 0]
         return (self.op, q[0], q[1], q[2])
 
     def __eq__(self, other) -> bool:
-        return isinstance(other, QuantumGate) and self.op == other.op and self.qubits == other.qubits
+        return isinstance(other, QuantumGate) and self.op == other.op and self._q == other._q
+
+    def __str__(self) -> str:  # QuantumGate Display (crates/necstar/src/circuit/gates.rs:329-347)
+        return f"{self.name}({', '.join(map(str, self._q))})"
 
     def __repr__(self) -> str:
-        return f"{self.name}({', '.join(map(str, self.qubits))})"
+        return f"<QuantumGate: {self}>"
 
     # constructors (python/necstar/gate.pyi)
     @staticmethod

@@ -1175,7 +1175,7 @@ nsg_status nsg_probe_int_ops(uint64_t iters, double* seconds, uint64_t* ops) {
     CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
     const int sms = device_sm_count(), threads = 256, blocks = sms * 8;
     uint32_t* sink = nullptr;
-    CK(cudaMalloc((void**)&sink, blocks * sizeof(uint32_t)));
+    CK(cudaMalloc((void**)&sink, (size_t)blocks * threads * sizeof(uint32_t)));
     CK(launch_int_probe(2, blocks, threads, sink, st));  // warm-up
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));

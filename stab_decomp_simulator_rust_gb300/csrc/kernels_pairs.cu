@@ -525,21 +525,32 @@ cudaError_t launch_pairs_w(const PairLaunch& p, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-// Eight independent 32-bit logic chains per thread: each step is one LOP3
-// (a ^ (b & c)) per chain.
+// Eight independent 32-bit logic chains per thread; every step is one
+// three-input logic op (lop3.b32, truth table 0x78 = a ^ (b & c)) per chain,
+// issued as volatile inline PTX so no step is folded away; the loop index
+// enters once per 128 ops so iterations cannot be collapsed, and every
+// thread stores its result.
+__device__ __forceinline__ uint32_t lop3_78(uint32_t a, uint32_t b, uint32_t c) {
+    uint32_t d;
+    asm volatile("lop3.b32 %0, %1, %2, %3, 0x78;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 __global__ void int_probe_kernel(uint64_t iters, uint32_t* sink) {
     uint32_t a0 = threadIdx.x, a1 = a0 * 3u + 1u, a2 = a0 * 5u + 7u, a3 = a0 * 7u + 3u;
     uint32_t a4 = a0 ^ 0x9e3779b9u, a5 = a1 ^ 0x7f4a7c15u, a6 = a2 ^ 0x85ebca6bu, a7 = a3 ^ 0xc2b2ae35u;
-    const uint32_t k1 = blockIdx.x | 0x1234u, k2 = blockIdx.x ^ 0xfeedu;
+    const uint32_t k = blockIdx.x | 0x1234u;
     for (uint64_t i = 0; i < iters; i++) {
+        a0 ^= (uint32_t)i;
 #pragma unroll
-        for (int u = 0; u < 16; u++) {
-            a0 = a0 ^ (a1 & k1); a1 = a1 ^ (a2 | k2); a2 = a2 ^ (a3 & k2); a3 = a3 ^ (a4 | k1);
-            a4 = a4 ^ (a5 & k1); a5 = a5 ^ (a6 | k2); a6 = a6 ^ (a7 & k2); a7 = a7 ^ (a0 | k1);
+        for (int u = 0; u < 16; u++) {  // 8 independent ops per round, rounds chained
+            uint32_t b0 = lop3_78(a0, a1, a2), b1 = lop3_78(a1, a2, a3), b2 = lop3_78(a2, a3, a4);
+            uint32_t b3 = lop3_78(a3, a4, a5), b4 = lop3_78(a4, a5, a6), b5 = lop3_78(a5, a6, a7);
+            uint32_t b6 = lop3_78(a6, a7, a0), b7 = lop3_78(a7, a0, k);
+            a0 = b0; a1 = b1; a2 = b2; a3 = b3; a4 = b4; a5 = b5; a6 = b6; a7 = b7;
         }
     }
-    uint32_t r = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
-    if (r == 0x5a5a5a5au) sink[blockIdx.x] = r;  // keeps the chains live
+    sink[blockIdx.x * blockDim.x + threadIdx.x] = a0 ^ a1 ^ a2 ^ a3 ^ a4 ^ a5 ^ a6 ^ a7;
 }
 
 }  // namespace

@@ -82,6 +82,8 @@ class PauliString:
 
     def __str__(self) -> str:
         inv = "IXYZ"
+        if self.kind == SPARSE and len(self.ops) == 0:
+            return "I"
         if self.kind == DENSE:
             return "".join(inv[o] for o in self.ops[::-1])
         return " ".join(f"{inv[o]}{q}" for o, q in zip(self.ops, self.qubits))
