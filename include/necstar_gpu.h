@@ -194,6 +194,18 @@ nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states
                                const nsg_pauli* paulis, const uint64_t* pauli_offsets,
                                uint32_t precision, double* out);
 
+/* ⟨P⟩ for callers that cannot allocate device memory at call time — a
+ * process whose GPU memory is already fully reserved by another allocator,
+ * or a latency-critical loop where cudaMalloc/cudaFree would synchronise the
+ * device.  Same value as nsg_exp_value; no counterpart in the reference.
+ * All scratch comes from one 16 MiB static device array (held by every GPU
+ * that loads the library until exit): n ≤ 64 and χ ≤ 8192, larger states give
+ * NSG_ERR_BUFFER_TOO_SMALL.  The first call on a device looks up the array's
+ * address (make it before any stream capture); all calls share the array,
+ * so calls that overlap on the GPU race.  Synchronous: *out is a host
+ * double. */
+nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pauli* pauli, double* out);
+
 /* QuantumState::inner_product ⟨a|b⟩ (crates/necstar/src/state/mod.rs:165-172 →
  * stabilizer_decomposed_state/inner_product.rs:9-19).  out = {re, im}. */
 nsg_status nsg_inner_product(const nsg_state* a, const nsg_state* b, double out[2]);

@@ -64,6 +64,7 @@ def load(path: str | None = None):
     L.nsg_apply_gates.argtypes = [vp, vp, sz]
     L.nsg_exp_value.argtypes = [vp, P(PauliABI), P(dbl)]
     L.nsg_exp_value_batch.argtypes = [vp, P(PauliABI), sz, u32, vp]
+    L.nsg_exp_value_noalloc.argtypes = [vp, P(PauliABI), P(dbl)]
     L.nsg_exp_value_multi.argtypes = [vp, sz, P(PauliABI), vp, u32, vp]
     L.nsg_inner_product.argtypes = [vp, vp, vp]
     L.nsg_norm.argtypes = [vp, P(dbl)]

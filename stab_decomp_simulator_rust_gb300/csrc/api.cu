@@ -1219,3 +1219,27 @@ nsg_status nsg_debug_pair_values(const nsg_state* cstate, const nsg_pauli* pauli
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Read-only access to a state and to the error slot for other translation
+// units of this library (noalloc.cu).
+namespace nsg {
+
+bool state_internals(const nsg_state* s, TermsView* tv, cudaStream_t* st, int** status, int* device, double* gf2) {
+    if (!s) return false;
+    *tv = s->t.view();
+    *st = s->st;
+    *status = s->status.p;
+    *device = s->device;
+    *gf2 = s->gf_re * s->gf_re + s->gf_im * s->gf_im;
+    return true;
+}
+
+void set_last_error(const char* msg, int64_t a, int64_t b) {
+    g_msg = msg;
+    g_args[0] = a;
+    g_args[1] = b;
+    g_args[2] = -1;
+}
+
+}  // namespace nsg
