@@ -406,13 +406,27 @@ struct nsg_state {
     bool frames_ok = false;
     DBuf<uint64_t> fGV, fFV, fMV, fGVL, fGVH;
     DBuf<int> status;
+    // cached ket tables (Four-Russians tables of every term, n ≤ 64)
+    bool ket_ok = false;
+    DBuf<unsigned char> ktab;
+
+    const void* ket_tables() {
+        if (!ket_ok) {
+            ktab.alloc(std::max<size_t>((size_t)t.chi, 1) * ket_table_stride(t.n), st);
+            CK(launch_ket_tables(t.view(), ktab.p, st));
+            ket_ok = true;
+        }
+        return ktab.p;
+    }
 
     void init_stream() {
         CK(cudaGetDevice(&device));
         CK(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
         st = own;
-        status.alloc(1, st);
-        CK(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+        // [0] status bits, [1] detail claimed, [2..4] where the first
+        // invariant was seen (kernel-specific: pair i, j and qubit).
+        status.alloc(8, st);
+        CK(cudaMemsetAsync(status.p, 0, 8 * sizeof(int), st));
     }
     ~nsg_state() {
         // Finish work on the current stream, then free everything on our own.
@@ -424,6 +438,8 @@ struct nsg_state {
         fGVL.rehome(own);
         fGVH.rehome(own);
         status.rehome(own);
+        ktab.rehome(own);
+        ktab.release();
         t = TermStore();
         fGV.release();
         fFV.release();
@@ -436,7 +452,10 @@ struct nsg_state {
             cudaStreamDestroy(own);
         }
     }
-    void invalidate() { frames_ok = false; }
+    void invalidate() {
+        frames_ok = false;
+        ket_ok = false;
+    }
     FrameView frames() {
         if (!frames_ok) {
             size_t cap = (size_t)std::max<int64_t>(t.chi, 1);
@@ -453,16 +472,18 @@ struct nsg_state {
     }
     // Reads and clears the device status word; maps it to an API error.
     void check_status(int64_t qubit = -1) {
-        int h = 0;
-        CK(cudaMemcpyAsync(&h, status.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        int h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        CK(cudaMemcpyAsync(h, status.p, sizeof(h), cudaMemcpyDeviceToHost, st));
         CK(cudaStreamSynchronize(st));
-        if (h) {
-            CK(cudaMemsetAsync(status.p, 0, sizeof(int), st));
+        if (h[0]) {
+            CK(cudaMemsetAsync(status.p, 0, sizeof(h), st));
             CK(cudaStreamSynchronize(st));
-            if (h & DS_CANNOT_DISCARD)
+            if (h[0] & DS_CANNOT_DISCARD)
                 raise(NSG_ERR_CANNOT_DISCARD_QUBIT, qubit, -1, "Cannot discard qubit %lld because it is not in a proper state",
                       (long long)qubit);
-            raise(NSG_ERR_DEVICE_INVARIANT, h, -1, "device invariant violated (status %d)", h);
+            if (h[0] & DS_TIMEOUT) raise(NSG_ERR_TIMEOUT, h[0], -1, "a bounded device wait ran out (status %d)", h[0]);
+            raise(NSG_ERR_DEVICE_INVARIANT, h[0], -1, "device invariant violated (status %d; at %d %d %d)", h[0], h[2],
+                  h[3], h[4]);
         }
     }
 };
@@ -568,6 +589,17 @@ void run_pairs(nsg_state* a, nsg_state* b, const std::vector<DevPauli>& paulis, 
     pl.status = a->status.p;
     pl.dbg_k = dbg_k;
     pl.dbg_r = dbg_r;
+    pl.ktab = b->ket_tables();  // produced on b's stream when first needed
+    if (b != a) {               // order this stream after b's table build
+        cudaEvent_t ev;
+        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        CK(cudaEventRecord(ev, b->st));
+        CK(cudaStreamWaitEvent(st, ev, 0));
+        cudaEventDestroy(ev);
+    }
+    pl.ktab_stride = ket_table_stride(b->t.n);
+    pl.ngrp = ket_table_groups(b->t.n);
+    pl.warp_smem = pair_warp_smem(b->t.n);
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool prof;
     {
@@ -878,6 +910,7 @@ nsg_status nsg_state_set_stream(nsg_state* state, void* cuda_stream) {
     state->fGVL.rehome(state->st);
     state->fGVH.rehome(state->st);
     state->status.rehome(state->st);
+    state->ktab.rehome(state->st);
     API_END
 }
 

@@ -66,6 +66,7 @@ enum DevStatus : int {
     DS_OK = 0,
     DS_INVARIANT = 1,  // reference panic paths
     DS_CANNOT_DISCARD = 2,
+    DS_TIMEOUT = 4,  // a bounded wait on a shared-memory barrier ran out
 };
 
 // ---- launchers (kernels_*.cu) ------------------------------------------------
@@ -128,11 +129,26 @@ struct PairLaunch {
     int blocks = 0;
     int warps_per_block = 4;
     int* status = nullptr;
+    const void* ktab = nullptr;  // ket tables of B ([chiB] x ket_table_stride bytes)
+    size_t ktab_stride = 0;
+    int ngrp = 0;
+    size_t warp_smem = 0;        // dynamic shared memory per warp (pair_warp_smem)
     uint8_t* dbg_k = nullptr;   // optional per-pair dump [chiA][chiB]
     int32_t* dbg_r = nullptr;
 };
 
 cudaError_t launch_pairs(const PairLaunch& p, cudaStream_t st);
+
+// The same sums with B's rows staged per pair instead of ket tables (no
+// per-term table storage; at most 32 observables).
+cudaError_t launch_pairs_rows(const PairLaunch& p, cudaStream_t st);
+
+// Ket tables: per term, Four-Russians tables of G, F, M and the ordered-sign
+// matrix P (n ≤ 64); sizes below.
+int ket_table_groups(int n);
+size_t ket_table_stride(int n);
+size_t pair_warp_smem(int n);
+cudaError_t launch_ket_tables(const TermsView& t, void* out, cudaStream_t st);
 
 // Reduce per-warp partials to one value (re, im) per observable, scaled by
 // `scale` (|global factor|² or the complex conj(g_a)·g_b).

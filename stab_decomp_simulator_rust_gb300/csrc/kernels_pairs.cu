@@ -33,7 +33,8 @@ namespace {
 
 using dev::FULL;
 using dev::popc;
-using dev::WarpCH;
+using dev::ffs0;
+using dev::shfl;
 
 constexpr int FWARPS = 4;  // warps per block in the frame kernels
 constexpr int PWARPS = 4;  // warps per block in the pair kernel
@@ -252,9 +253,445 @@ struct ChunkAcc {
     }
 };
 
+// ---- ket tables -----------------------------------------------------------------
+// Per term B: Four-Russians tables of its rows, 16 XOR combinations of each
+// group of four rows, for the matrices G, F, M and P, where P[q] holds the
+// bits r > q with parity(M_q·F_r) (so that Σ_{q<r∈f} M_q·F_r =
+// parity((f·P) ∧ f)).  Layout per term: [4][ngrp][16] Words.
+template <typename Word>
+__global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, int ngrp, Word* __restrict__ out) {
+    __shared__ Word sR[FWARPS][4][64];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t term = (int64_t)blockIdx.x * FWARPS + wid;
+    if (term >= tv.chi) return;
+    const int n = tv.n;
+    for (int r = lane; r < 64; r += 32) {
+        size_t idx = ((size_t)term * tv.R + r) * tv.W;
+        sR[wid][0][r] = (Word)tv.G[idx];
+        sR[wid][1][r] = (Word)tv.F[idx];
+        sR[wid][2][r] = (Word)tv.M[idx];
+    }
+    __syncwarp();
+    for (int q = lane; q < 64; q += 32) {
+        Word pq = 0;
+        if (q < n) {
+            const Word mq = sR[wid][2][q];
+            for (int r = q + 1; r < n; r++) pq |= (Word)(popc<Word>(mq & sR[wid][1][r]) & 1) << r;
+        }
+        sR[wid][3][q] = pq;
+    }
+    __syncwarp();
+    const int per = ngrp * 16, total = 4 * per;
+    Word* dst = out + (size_t)term * total;
+    for (int e = lane; e < total; e += 32) {
+        const int mat = e / per, g = (e / 16) % ngrp, idx = e & 15;
+        Word acc = 0;
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const int row = 4 * g + b;
+            if (((idx >> b) & 1) && row < n) acc ^= sR[wid][mat][row];
+        }
+        dst[e] = acc;
+    }
+}
+
+// ---- pair kernel ---------------------------------------------------------------
+// Shared memory per warp: two table buffers (double-buffered TMA bulk copies
+// of the next ket's tables), the transformed ket's F and M rows, and one
+// mbarrier per buffer.
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// One elected lane: arm the barrier for `bytes` and start the bulk copy.
+__device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait on a barrier phase; false if the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); it++) {
+        uint32_t done;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+template <typename Word>
+__device__ __forceinline__ Word lsb(Word x) {  // lowest set bit as a mask
+    return x & ((Word)0 - x);
+}
+
+template <typename Word>
+__device__ __forceinline__ int parity(Word x) {
+    return popc<Word>(x) & 1;
+}
+
+// left_multiply_h (h.rs:13-65) + _resolve_superposition (resolve_superposition.rs:6-176)
+// on a warp-held tableau with one word per row.  The commuting column
+// operations of the basis transform are applied as one masked update; the
+// pivot is the lowest set bit of D0 (else D1), as in the reference.
+template <typename Word, int RPL>
+__device__ __forceinline__ void pair_h(Word (&G)[RPL], Word (&F)[RPL], Word (&M)[RPL], uint32_t& gam, Word& v,
+                                       Word& s, int& phase, int q, int& err) {
+    const int sl = q >> 5, src = q & 31;
+    Word g0 = G[0], f0 = F[0], m0 = M[0];
+    uint32_t gg = gam;
+    if (RPL > 1 && sl) {
+        g0 = G[RPL - 1];
+        f0 = F[RPL - 1];
+        m0 = M[RPL - 1];
+        gg = gam >> 2;
+    }
+    const Word Gq = shfl<Word>(g0, src), Fq = shfl<Word>(f0, src), Mq = shfl<Word>(m0, src);
+    const int gq = (int)(shfl<uint32_t>(gg, src) & 3);
+    const Word nv = ~v;
+    const Word t = s ^ (Gq & v);
+    const Word u = s ^ (Fq & nv) ^ (Mq & v);
+    const int alpha = parity<Word>(Gq & nv & s);
+    const int beta = parity<Word>((Mq & nv & s) ^ (Fq & v & (Mq ^ s)));
+    const int delta = (2 * gq + 4 * (alpha ^ beta)) & 7;
+    phase = (phase + 4 * alpha) & 7;
+    const Word d = t ^ u;
+    if (d == 0) {  // handle_same_vecs_case :115-133
+        if (delta == 4) err = 1;
+        s = t;
+        phase = (phase + (delta == 2 ? 1 : (delta == 6 ? 7 : 0))) & 7;
+        return;
+    }
+    const Word d0 = d & nv, d1 = d & v;
+    Word pm;
+    if (d0) {
+        pm = lsb<Word>(d0);
+        const Word rest = d0 ^ pm;
+#pragma unroll
+        for (int k = 0; k < RPL; k++) {
+            const bool fb = (F[k] & pm) != 0;
+            const int par1 = parity<Word>(F[k] & d1);
+            if (parity<Word>(G[k] & rest)) G[k] ^= pm;
+            if (parity<Word>(M[k] & rest) ^ par1) M[k] ^= pm;
+            if (fb) {
+                F[k] ^= rest;
+                M[k] ^= d1;
+                if (par1) gam ^= 2u << (2 * k);
+            }
+        }
+    } else {
+        pm = lsb<Word>(d1);
+        const Word rest = d1 ^ pm;
+#pragma unroll
+        for (int k = 0; k < RPL; k++) {
+            if (G[k] & pm) G[k] ^= rest;
+            if (parity<Word>(F[k] & rest)) F[k] ^= pm;
+            if (M[k] & pm) M[k] ^= rest;
+        }
+    }
+    const bool vp = (v & pm) != 0;
+    s = (t & pm) ? u : t;
+    bool sp, vnew = vp, rs = false;
+    int dph = 0;
+    if (t & pm) {
+        switch (delta) {
+            case 0: sp = false; vnew = !vp; break;
+            case 4: sp = true; vnew = !vp; dph = 4; break;
+            case 2: if (vp) { dph = 1; sp = false; } else { sp = true; vnew = true; dph = 2; } rs = true; break;
+            default: if (vp) { dph = 7; sp = true; } else { sp = false; vnew = true; dph = 6; } rs = true; break;
+        }
+    } else {
+        switch (delta) {
+            case 0: sp = false; vnew = !vp; break;
+            case 4: sp = true; vnew = !vp; break;
+            case 2: if (vp) { dph = 1; sp = true; } else { sp = false; vnew = true; } rs = true; break;
+            default: if (vp) { dph = 7; sp = false; } else { sp = true; vnew = true; } rs = true; break;
+        }
+    }
+    s = sp ? (s | pm) : (s & ~pm);
+    v = vnew ? (v | pm) : (v & ~pm);
+    phase = (phase + dph) & 7;
+    if (rs) {  // right_multiply_s(pivot) (right_multiplication/s.rs:8-24)
+#pragma unroll
+        for (int k = 0; k < RPL; k++) {
+            if (F[k] & pm) {
+                M[k] ^= pm;
+                const uint32_t gk = (gam >> (2 * k)) & 3;
+                gam = (gam & ~(3u << (2 * k))) | (((gk + 3) & 3) << (2 * k));
+            }
+        }
+    }
+}
+
+template <typename Word, int RPL>
+__device__ __forceinline__ int nib(const Word x, int g) {  // 4-bit group g of a row
+    return (int)((x >> (4 * g)) & 15);
+}
+
 template <typename Word, int RPL, int NG>
-__global__ void __launch_bounds__(PWARPS * 32) pair_kernel(PairLaunch p) {
-    using Eng = WarpCH<Word, 1, RPL>;
+__global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
+    constexpr int GMAX = (8 * sizeof(Word)) / 4;  // groups of four rows (8 or 16)
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int gwarp = blockIdx.x * PWARPS + wid;
+    unsigned char* wbase = smem_raw + (size_t)wid * p.warp_smem;
+    const uint32_t tab_bytes = (uint32_t)p.ktab_stride;
+    Word* tb0 = (Word*)wbase;
+    Word* tb1 = (Word*)(wbase + tab_bytes);
+    Word* sF = (Word*)(wbase + 2 * tab_bytes);
+    Word* sM = sF + 64;
+    uint64_t* bars = (uint64_t*)(sM + 64);
+    if (lane == 0) {
+        mbar_init(&bars[0]);
+        mbar_init(&bars[1]);
+        fence_mbar_init();
+    }
+    __syncwarp();
+    uint32_t par0 = 0, par1 = 0;  // next phase parity per buffer
+    const unsigned char* ktab = (const unsigned char*)p.ktab;
+
+    const TermsView& A = p.A;
+    const TermsView& Bt = p.B;
+    const int n = A.n, ngrp = p.ngrp;
+    const int64_t chiA = A.chi, chiB = Bt.chi;
+    const int nobs = p.nobs;
+
+    int64_t cur_i = -1;
+    Word GV[RPL], FV[RPL], MV[RPL];
+    uint32_t gamV = 0;
+    Word vA = 0, sA = 0;
+    int kcA = 0, rcA = 0;
+    Word xs[NG];
+    int ks[NG];
+    const int64_t cpr = p.triangular ? 0 : (chiB + p.chunk - 1) / p.chunk;
+    int buf = 0;
+    bool timed_out = false;
+
+    for (int64_t c = gwarp; c < p.total_chunks && !timed_out; c += p.nwarps) {
+        int64_t i, j0, j1;
+        if (p.triangular) {
+            int64_t lo = 0, hi = chiA;
+            while (hi - lo > 1) {
+                int64_t mid = (lo + hi) >> 1;
+                if (p.row_chunk_off[mid] <= c) lo = mid;
+                else hi = mid;
+            }
+            i = lo;
+            j0 = i + (c - p.row_chunk_off[i]) * p.chunk;
+        } else {
+            i = c / cpr;
+            j0 = (c % cpr) * p.chunk;
+        }
+        j1 = min(j0 + (int64_t)p.chunk, chiB);
+        if (i != cur_i) {
+            cur_i = i;
+#pragma unroll
+            for (int k = 0; k < RPL; k++) {
+                size_t o = (size_t)i * 64 + 32 * k + lane;
+                GV[k] = (Word)p.fr.GV[o];
+                FV[k] = (Word)p.fr.FV[o];
+                MV[k] = (Word)p.fr.MV[o];
+            }
+            const uint64_t gvl = p.fr.GVL[i], gvh = p.fr.GVH[i];
+            gamV = 0;
+#pragma unroll
+            for (int k = 0; k < RPL; k++) {
+                const int r = 32 * k + lane;
+                gamV |= (uint32_t)(((gvl >> r) & 1) | (((gvh >> r) & 1) << 1)) << (2 * k);
+            }
+            vA = (Word)A.V[i * A.W];
+            sA = (Word)A.S[i * A.W];
+            kcA = A.coef_k[i];
+            rcA = A.coef_r[i];
+#pragma unroll
+            for (int g = 0; g < NG; g++) {
+                const int o = 32 * g + lane;
+                xs[g] = (o < nobs) ? (Word)p.px[(size_t)i * nobs + o] : (Word)0;
+                ks[g] = (o < nobs) ? p.pk[(size_t)i * nobs + o] : 0;
+            }
+        }
+        constexpr int NA = (NG == 1) ? 4 : 2;
+        ChunkAcc<NG, NA> acc;
+        acc.reset();
+
+        // first ket of the chunk
+        if (lane == 0) {
+            fence_proxy_async();
+            tma_load(buf ? tb1 : tb0, ktab + (size_t)j0 * tab_bytes, tab_bytes, buf ? &bars[1] : &bars[0]);
+        }
+        for (int64_t j = j0; j < j1; j++) {
+            // prefetch the next ket's tables into the other buffer
+            if (j + 1 < j1 && lane == 0) {
+                fence_proxy_async();
+                tma_load(buf ? tb0 : tb1, ktab + (size_t)(j + 1) * tab_bytes, tab_bytes, buf ? &bars[0] : &bars[1]);
+            }
+            const Word glB = (Word)Bt.GL[j * Bt.W], ghB = (Word)Bt.GH[j * Bt.W];
+            Word v = (Word)Bt.V[j * Bt.W], s = (Word)Bt.S[j * Bt.W];
+            int phase = Bt.phase[j];
+            const int kcB = Bt.coef_k[j], rcB = Bt.coef_r[j];
+            bool ok_wait;
+            if (buf) {
+                ok_wait = mbar_wait(&bars[1], par1);
+                par1 ^= 1;
+            } else {
+                ok_wait = mbar_wait(&bars[0], par0);
+                par0 ^= 1;
+            }
+            if (!ok_wait) {
+                // Record the timeout, then give the prefetch into the other
+                // buffer (if one was issued) a bounded wait before leaving.
+                if (lane == 0) atomicOr(p.status, DS_TIMEOUT);
+                if (j + 1 < j1) {
+                    if (buf) mbar_wait(&bars[0], par0);
+                    else mbar_wait(&bars[1], par1);
+                }
+                timed_out = true;
+                break;
+            }
+            const Word* T = buf ? tb1 : tb0;
+
+            // ---- D = V·U_B by table lookups (Four Russians)
+            Word gD[RPL], fD[RPL], mD[RPL], y[RPL];
+#pragma unroll
+            for (int k = 0; k < RPL; k++) gD[k] = fD[k] = mD[k] = y[k] = 0;
+#pragma unroll
+            for (int g = 0; g < GMAX; g++) {
+                if (g < ngrp) {
+                    const Word* TG = T + g * 16;
+                    const Word* TF = T + (ngrp + g) * 16;
+                    const Word* TM = T + (2 * ngrp + g) * 16;
+                    const Word* TP = T + (3 * ngrp + g) * 16;
+#pragma unroll
+                    for (int k = 0; k < RPL; k++) {
+                        const int ig = nib<Word, RPL>(GV[k], g), jf = nib<Word, RPL>(FV[k], g),
+                                  im = nib<Word, RPL>(MV[k], g);
+                        gD[k] ^= TG[ig];
+                        fD[k] ^= TF[jf];
+                        mD[k] ^= TM[jf] ^ TG[im];
+                        y[k] ^= TP[jf];
+                    }
+                }
+            }
+            uint32_t gam = 0;
+#pragma unroll
+            for (int k = 0; k < RPL; k++) {
+                const int gsum = popc<Word>(FV[k] & glB) + 2 * popc<Word>(FV[k] & ghB);
+                const int g = (int)((gamV >> (2 * k)) & 3) + gsum + 2 * parity<Word>(y[k] & FV[k]);
+                gam |= (uint32_t)(g & 3) << (2 * k);
+            }
+
+            // ---- U_{H,A}
+            int err = 0;
+            Word hv = vA;
+            int errq = -1;
+            while (hv) {
+                const int q = ffs0<Word>(hv);
+                hv &= hv - 1;
+                pair_h<Word, RPL>(gD, fD, mD, gam, v, s, phase, q, err);
+                if (err && errq < 0) errq = q;
+            }
+            if (err && lane == 0) {
+                atomicOr(p.status, DS_INVARIANT);
+                if (atomicCAS(p.status + 1, 0, 1) == 0) {  // first hit: record where
+                    p.status[2] = (int)i;
+                    p.status[3] = (int)j;
+                    p.status[4] = errq;
+                }
+            }
+
+            // ---- stage F, M rows of the transformed ket; γ planes by ballot
+#pragma unroll
+            for (int k = 0; k < RPL; k++) {
+                sF[32 * k + lane] = fD[k];
+                sM[32 * k + lane] = mD[k];
+            }
+            Word gl2 = 0, gh2 = 0;
+#pragma unroll
+            for (int k = 0; k < RPL; k++) {
+                const uint32_t b0 = __ballot_sync(FULL, gam & (1u << (2 * k)));
+                const uint32_t b1 = __ballot_sync(FULL, gam & (2u << (2 * k)));
+                gl2 |= (Word)b0 << (32 * k);
+                gh2 |= (Word)b1 << (32 * k);
+            }
+            __syncwarp();
+            const int rv = popc<Word>(v);
+
+            // ---- amplitudes ⟨x|ket⟩: u = xF, m = xM, ordered sign Σ_{p<r∈x} M_p·F_r
+            //      (parity accumulated as an XOR of the masked products).
+            Word u[NG], mac[NG], sacc[NG];
+#pragma unroll
+            for (int g = 0; g < NG; g++) u[g] = mac[g] = sacc[g] = 0;
+            for (int q = 0; q < n; q++) {
+                const Word f = sF[q], m = sM[q];
+                const Word bit = (Word)1 << q;
+#pragma unroll
+                for (int g = 0; g < NG; g++) {
+                    const Word sel = (xs[g] & bit) ? ~(Word)0 : (Word)0;
+                    const Word fs = f & sel;
+                    sacc[g] ^= mac[g] & fs;
+                    mac[g] ^= m & sel;
+                    u[g] ^= fs;
+                }
+            }
+            const int kpair = (kcB - kcA) & 7;
+            const int rpair = rcA + rcB + rv;
+            const int wgt = (p.triangular && j != i) ? 2 : 1;
+#pragma unroll
+            for (int g = 0; g < NG; g++) {
+                const int o = 32 * g + lane;
+                const bool ok = (((u[g] ^ s) & ~v) == 0);
+                const int gsum = popc<Word>(xs[g] & gl2) + 2 * popc<Word>(xs[g] & gh2);
+                const int sg = parity<Word>(sacc[g] ^ (u[g] & mac[g]) ^ (u[g] & v & s));
+                const int kamp = (phase + 2 * gsum + 4 * sg) & 7;
+                if (p.dbg_k && o == 0) {
+                    const size_t di = (size_t)i * chiB + j;
+                    p.dbg_k[di] = ok ? (uint8_t)((ks[g] + kamp) & 7) : (uint8_t)255;
+                    p.dbg_r[di] = rv;
+                }
+                if (ok && o < nobs) {
+                    double* pp = p.partials + ((size_t)gwarp * nobs + o) * 8;
+                    const int k = (kpair + ks[g] + kamp) & 7;
+                    int sgn, m;
+                    re_part(k, rpair, sgn, m);
+                    if (sgn) acc.add(g, m & 1, sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1), p.mixed, pp);
+                    if (NA == 4 && p.complex_out) {
+                        im_part(k, rpair, sgn, m);
+                        if (sgn)
+                            acc.add(g, (NA == 4 ? 2 : 0) + (m & 1), sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1),
+                                    p.mixed, pp);
+                    }
+                }
+            }
+            __syncwarp();  // all lanes done with buffer `buf` and the staged rows
+            buf ^= 1;
+        }
+        // ---- flush the chunk into this warp's double-double partials
+#pragma unroll
+        for (int g = 0; g < NG; g++) {
+            const int o = 32 * g + lane;
+            if (o < nobs) acc.flush_group(g, p.partials + ((size_t)gwarp * nobs + o) * 8, p.mixed);
+        }
+    }
+}
+
+// Row-staged variant of the pair kernel (no ket tables): B's rows are
+// staged in shared memory and composed bit by bit.  It needs no per-term
+// table storage, which is what nsg_exp_value_noalloc's fixed scratch
+// affords; one observable per lane group.
+template <typename Word, int RPL, int NG>
+__global__ void __launch_bounds__(PWARPS * 32) pair_kernel_rows(PairLaunch p) {
+    using Eng = dev::WarpCH<Word, 1, RPL>;
     __shared__ Word sGs[PWARPS][64], sFs[PWARPS][64], sMs[PWARPS][64];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gwarp = blockIdx.x * PWARPS + wid;
@@ -513,16 +950,28 @@ __global__ void reduce_kernel(const double* __restrict__ partials, int nwarps, i
     }
 }
 
+template <typename Word, int RPL, int NG>
+cudaError_t launch_pairs_ng(const PairLaunch& p, cudaStream_t st) {
+    const size_t smem = (size_t)p.warp_smem * PWARPS;
+    static size_t configured = 0;  // per instantiation: raise the dynamic shared-memory limit once
+    if (smem > 48 * 1024 && configured < smem) {
+        cudaError_t e = cudaFuncSetAttribute(pair_kernel<Word, RPL, NG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = smem;
+    }
+    pair_kernel<Word, RPL, NG><<<p.blocks, PWARPS * 32, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
 template <typename Word, int RPL>
 cudaError_t launch_pairs_w(const PairLaunch& p, cudaStream_t st) {
-    int ng = (p.nobs + 31) / 32;
-    dim3 grid(p.blocks), block(PWARPS * 32);
-    if (ng <= 1) pair_kernel<Word, RPL, 1><<<grid, block, 0, st>>>(p);
-    else if (ng <= 2) pair_kernel<Word, RPL, 2><<<grid, block, 0, st>>>(p);
-    else if (ng <= 4) pair_kernel<Word, RPL, 4><<<grid, block, 0, st>>>(p);
-    else if (ng <= 8) pair_kernel<Word, RPL, 8><<<grid, block, 0, st>>>(p);
-    else return cudaErrorInvalidValue;
-    return cudaGetLastError();
+    const int ng = (p.nobs + 31) / 32;
+    if (ng <= 1) return launch_pairs_ng<Word, RPL, 1>(p, st);
+    if (ng <= 2) return launch_pairs_ng<Word, RPL, 2>(p, st);
+    if (ng <= 4) return launch_pairs_ng<Word, RPL, 4>(p, st);
+    if (ng <= 8) return launch_pairs_ng<Word, RPL, 8>(p, st);
+    return cudaErrorInvalidValue;
 }
 
 // Eight independent 32-bit logic chains per thread; every step is one
@@ -571,6 +1020,37 @@ cudaError_t launch_pauli_frames(const TermsView& t, const DevPauli* d_paulis, in
     if (t.chi == 0 || nobs == 0) return cudaSuccess;
     pauli_frames_kernel<<<(unsigned)((t.chi + FWARPS - 1) / FWARPS), FWARPS * 32, 0, st>>>(t, d_paulis, nobs, x_out,
                                                                                           k_out);
+    return cudaGetLastError();
+}
+
+int pair_word_bytes(int n) { return n <= 32 ? 4 : 8; }
+
+size_t ket_table_stride(int n) {  // bytes per term: [4][ngrp][16] words
+    return (size_t)4 * ket_table_groups(n) * 16 * pair_word_bytes(n);
+}
+
+int ket_table_groups(int n) { return n <= 0 ? 1 : (n + 3) / 4; }
+
+size_t pair_warp_smem(int n) {
+    size_t b = 2 * ket_table_stride(n) + 2 * 64 * (size_t)pair_word_bytes(n) + 2 * sizeof(uint64_t);
+    return (b + 127) & ~(size_t)127;
+}
+
+cudaError_t launch_ket_tables(const TermsView& t, void* out, cudaStream_t st) {
+    if (t.chi == 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((t.chi + FWARPS - 1) / FWARPS);
+    if (t.n <= 32)
+        ket_tables_kernel<uint32_t><<<blocks, FWARPS * 32, 0, st>>>(t, ket_table_groups(t.n), (uint32_t*)out);
+    else
+        ket_tables_kernel<uint64_t><<<blocks, FWARPS * 32, 0, st>>>(t, ket_table_groups(t.n), (uint64_t*)out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_rows(const PairLaunch& p, cudaStream_t st) {
+    if (p.total_chunks == 0) return cudaSuccess;
+    if (p.nobs > 32) return cudaErrorInvalidValue;
+    if (p.A.n <= 32) pair_kernel_rows<uint32_t, 1, 1><<<p.blocks, PWARPS * 32, 0, st>>>(p);
+    else pair_kernel_rows<uint64_t, 2, 1><<<p.blocks, PWARPS * 32, 0, st>>>(p);
     return cudaGetLastError();
 }
 

@@ -5,10 +5,11 @@
 // another allocator (a framework's caching allocator holding the whole GPU
 // fails every further cudaMalloc), or a latency-critical loop where
 // cudaMalloc/cudaFree would synchronise the device.  This entry point runs
-// the same kernels as nsg_exp_value (bra frames, Pauli frames, the pair
-// kernel, the FP64 reduction) but takes all of their scratch from one
-// file-scope device array, g_noalloc_scratch, of 16 MiB.  Every GPU that
-// loads the library holds that array until the process exits.
+// the kernels of nsg_exp_value (bra frames, Pauli frames, the pair sum, the
+// FP64 reduction; the pair sum in its row-staged form, which needs no
+// per-term ket tables) but takes all of their scratch from one file-scope
+// device array, g_noalloc_scratch, of 16 MiB.  Every GPU that loads the
+// library holds that array until the process exits.
 //
 // Limits: n ≤ 64 qubits and χ ≤ 8192 terms (the frames of 8192 terms plus
 // the pair-kernel partials fit the 16 MiB); larger states are rejected with
@@ -190,7 +191,7 @@ extern "C" nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pa
     if ((ce = cudaGetLastError()) != cudaSuccess) return cuda_fail(ce);
     if ((ce = launch_frames(tv, fr, st)) != cudaSuccess) return cuda_fail(ce);
     if ((ce = launch_pauli_frames(tv, dpp, 1, px, pk, st)) != cudaSuccess) return cuda_fail(ce);
-    if ((ce = launch_pairs(pl, st)) != cudaSuccess) return cuda_fail(ce);
+    if ((ce = launch_pairs_rows(pl, st)) != cudaSuccess) return cuda_fail(ce);
     if ((ce = launch_reduce(partials, pl.nwarps, 1, false, gf2, 0.0, dout, st)) != cudaSuccess) return cuda_fail(ce);
     double h = 0.0;
     int hs = 0;
