@@ -534,109 +534,266 @@ bool g_prof_on = false;
 double g_prof_ms = 0.0;
 uint64_t g_prof_launches = 0, g_prof_pairs = 0;
 
-// Σ-pairs driver: one launch over the pair space for `nobs` observables.
-void run_pairs(nsg_state* a, nsg_state* b, const std::vector<DevPauli>& paulis, bool triangular, bool complex_out,
-               bool mixed, std::vector<double>& out, uint8_t* dbg_k = nullptr, int32_t* dbg_r = nullptr) {
-    cudaStream_t st = a->st;
-    const int nobs = (int)paulis.size();
-    const int64_t chiA = a->t.chi, chiB = b->t.chi;
-    out.assign((size_t)nobs * (complex_out ? 2 : 1), 0.0);
-    if (nobs == 0 || chiA == 0 || chiB == 0) return;
-    FrameView fr = a->frames();
+// One pair sum of the batched driver: the χ_A×χ_B pair space of (a, b)
+// (triangular i ≤ j when a == b) for up to 256 observables.
+struct PairUnit {
+    nsg_state* a = nullptr;
+    nsg_state* b = nullptr;
+    const DevPauli* paulis = nullptr;  // host
+    int nobs = 0;
+    bool triangular = true;
+    bool complex_out = false;
+    double* out = nullptr;  // host: nobs values, or nobs (re, im) pairs when complex_out
+};
+
+constexpr int kPairChunk = 32;       // kets per chunk (one ket-table prefetch chain)
+constexpr int kMaxObsPerUnit = 256;  // 8 observable groups of 32 lanes
+
+// Orders `st` after all work queued so far on `other`.
+void join_stream(cudaStream_t st, cudaStream_t other) {
+    if (other == st) return;
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, other));
+    CK(cudaStreamWaitEvent(st, ev, 0));
+    cudaEventDestroy(ev);
+}
+
+// The batched Σ-pairs driver.  Every unit becomes one descriptor of a
+// persistent pair launch (one launch per word width: states of ≤ 32 qubits
+// run on 32-bit rows, wider ones on 64-bit rows), followed by one reduction
+// launch; all of it on `st`.  Bra frames and ket tables are built (once per
+// state, cached) on each state's own stream and joined into `st`.
+void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, uint8_t* dbg_k = nullptr,
+                    int32_t* dbg_r = nullptr) {
+    std::vector<PairUnit*> live;
+    for (auto& u : units) {
+        const size_t nout = (u.complex_out ? 2 : 1) * (size_t)u.nobs;
+        std::fill(u.out, u.out + nout, 0.0);
+        if (u.nobs > 0 && u.a->t.chi > 0 && u.b->t.chi > 0) live.push_back(&u);
+    }
+    if (live.empty()) return;
+    // Per-state caches on the states' streams, then join those streams.
+    std::vector<nsg_state*> touched;
+    for (PairUnit* u : live) {
+        u->a->frames();
+        u->b->ket_tables();
+        touched.push_back(u->a);
+        touched.push_back(u->b);
+    }
+    std::sort(touched.begin(), touched.end());
+    touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+    for (nsg_state* s : touched) join_stream(st, s->st);
+
+    // Observables and Pauli frames of every unit.
+    size_t tot_obs = 0, tot_px = 0;
+    for (PairUnit* u : live) {
+        tot_obs += (size_t)u->nobs;
+        tot_px += (size_t)u->a->t.chi * u->nobs;
+    }
+    std::vector<DevPauli> hp;
+    hp.reserve(tot_obs);
+    for (PairUnit* u : live) hp.insert(hp.end(), u->paulis, u->paulis + u->nobs);
     DBuf<DevPauli> dp;
-    dp.alloc(nobs, st);
-    CK(cudaMemcpyAsync(dp.p, paulis.data(), nobs * sizeof(DevPauli), cudaMemcpyHostToDevice, st));
+    dp.alloc(tot_obs, st);
+    CK(cudaMemcpyAsync(dp.p, hp.data(), tot_obs * sizeof(DevPauli), cudaMemcpyHostToDevice, st));
     DBuf<uint64_t> px;
     DBuf<uint8_t> pk;
-    px.alloc((size_t)chiA * nobs, st);
-    pk.alloc((size_t)chiA * nobs, st);
-    CK(launch_pauli_frames(a->t.view(), dp.p, nobs, px.p, pk.p, st));
+    px.alloc(tot_px, st);
+    pk.alloc(tot_px, st);
 
-    PairLaunch pl;
-    pl.A = a->t.view();
-    pl.fr = fr;
-    pl.B = b->t.view();
-    pl.px = px.p;
-    pl.pk = pk.p;
-    pl.nobs = nobs;
-    pl.triangular = triangular;
-    pl.complex_out = complex_out;
-    pl.mixed = mixed;
-    pl.chunk = 32;
-    std::vector<int64_t> off;
-    DBuf<int64_t> doff;
-    if (triangular) {
-        off.resize(chiA + 1);
-        off[0] = 0;
-        for (int64_t i = 0; i < chiA; i++) off[i + 1] = off[i] + (chiA - i + pl.chunk - 1) / pl.chunk;
-        pl.total_chunks = off[chiA];
-        doff.alloc(off.size(), st);
-        CK(cudaMemcpyAsync(doff.p, off.data(), off.size() * 8, cudaMemcpyHostToDevice, st));
-        pl.row_chunk_off = doff.p;
-    } else {
-        pl.total_chunks = chiA * ((chiB + pl.chunk - 1) / pl.chunk);
-    }
-    const int sms = device_sm_count();
-    const int wpb = 4;
-    int64_t want_blocks = (pl.total_chunks + wpb - 1) / wpb;
-    pl.blocks = (int)std::max<int64_t>(1, std::min<int64_t>(want_blocks, (int64_t)sms * 16));
-    pl.warps_per_block = wpb;
-    pl.nwarps = pl.blocks * wpb;
-    DBuf<double> partials;
-    partials.alloc((size_t)pl.nwarps * nobs * 8, st);
-    CK(cudaMemsetAsync(partials.p, 0, partials.n * sizeof(double), st));
-    pl.partials = partials.p;
-    pl.status = a->status.p;
-    pl.dbg_k = dbg_k;
-    pl.dbg_r = dbg_r;
-    pl.ktab = b->ket_tables();  // produced on b's stream when first needed
-    if (b != a) {               // order this stream after b's table build
-        cudaEvent_t ev;
-        CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-        CK(cudaEventRecord(ev, b->st));
-        CK(cudaStreamWaitEvent(st, ev, 0));
-        cudaEventDestroy(ev);
-    }
-    pl.ktab_stride = ket_table_stride(b->t.n);
-    pl.ngrp = ket_table_groups(b->t.n);
-    pl.warp_smem = pair_warp_smem(b->t.n);
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     bool prof;
     {
         std::lock_guard<std::mutex> lk(g_prof_mu);
         prof = g_prof_on;
     }
-    if (prof) {
-        CK(cudaEventCreate(&ev0));
-        CK(cudaEventCreate(&ev1));
-        CK(cudaEventRecord(ev0, st));
+    const int sms = device_sm_count();
+    std::vector<double> hout(2 * tot_obs, 0.0);
+    std::vector<DBuf<unsigned char>> keep_alive;  // per-launch descriptor buffers
+    std::vector<DBuf<double>> keep_rec;
+    float prof_ms = 0.f;
+    uint64_t prof_pairs = 0, prof_launches = 0;
+
+    size_t obs_base = 0, px_base = 0;
+    std::vector<size_t> unit_obs(live.size()), unit_px(live.size());
+    for (size_t k = 0; k < live.size(); k++) {
+        unit_obs[k] = obs_base;
+        unit_px[k] = px_base;
+        obs_base += (size_t)live[k]->nobs;
+        px_base += (size_t)live[k]->a->t.chi * live[k]->nobs;
+        CK(launch_pauli_frames(live[k]->a->t.view(), dp.p + unit_obs[k], live[k]->nobs, px.p + unit_px[k],
+                               pk.p + unit_px[k], st));
     }
-    CK(launch_pairs(pl, st));
+
+    for (int wb : {4, 8}) {
+        std::vector<size_t> sel;
+        for (size_t k = 0; k < live.size(); k++)
+            if ((live[k]->b->t.n <= 32 ? 4 : 8) == wb) sel.push_back(k);
+        if (sel.empty()) continue;
+        // Host descriptors; row-chunk prefixes of the triangular units in one buffer.
+        std::vector<PairDesc> descs(sel.size());
+        std::vector<int64_t> dbegin(sel.size() + 1, 0), obegin(sel.size() + 1, 0), offs;
+        std::vector<size_t> off_at(sel.size(), 0);
+        size_t tab_max = 0;
+        int nobs_max = 1;
+        for (size_t q = 0; q < sel.size(); q++) {
+            PairUnit* u = live[sel[q]];
+            const int64_t chiA = u->a->t.chi, chiB = u->b->t.chi;
+            PairDesc& d = descs[q];
+            d.A = u->a->t.view();
+            d.B = u->b->t.view();
+            d.fr = u->a->frames();
+            d.ktab = u->b->ket_tables();
+            d.ktab_stride = ket_table_stride(u->b->t.n);
+            d.ngrp = ket_table_groups(u->b->t.n);
+            d.nobs = u->nobs;
+            d.px = px.p + unit_px[sel[q]];
+            d.pk = pk.p + unit_px[sel[q]];
+            d.triangular = u->triangular ? 1 : 0;
+            d.complex_out = u->complex_out ? 1 : 0;
+            d.status = u->a->status.p;
+            if (u->complex_out) {  // conj(g_a)·g_b (stabilizer_decomposed_state/inner_product.rs:18)
+                d.scale_re = u->a->gf_re * u->b->gf_re + u->a->gf_im * u->b->gf_im;
+                d.scale_im = u->a->gf_re * u->b->gf_im - u->a->gf_im * u->b->gf_re;
+            } else {  // |g|² (exp_value.rs:60, norm.rs:29)
+                d.scale_re = u->a->gf_re * u->a->gf_re + u->a->gf_im * u->a->gf_im;
+                d.scale_im = 0.0;
+            }
+            int64_t nch;
+            if (u->triangular) {
+                off_at[q] = offs.size();
+                int64_t acc = 0;
+                for (int64_t i = 0; i < chiA; i++) {
+                    offs.push_back(acc);
+                    acc += (chiA - i + kPairChunk - 1) / kPairChunk;
+                }
+                offs.push_back(acc);
+                nch = acc;
+                prof_pairs += (uint64_t)(chiA * (chiA + 1) / 2);
+            } else {
+                d.cpr = (chiB + kPairChunk - 1) / kPairChunk;
+                nch = chiA * d.cpr;
+                prof_pairs += (uint64_t)(chiA * chiB);
+            }
+            dbegin[q + 1] = dbegin[q] + nch;
+            obegin[q + 1] = obegin[q] + u->nobs;
+            tab_max = std::max(tab_max, d.ktab_stride);
+            nobs_max = std::max(nobs_max, u->nobs);
+        }
+        const int64_t total = dbegin.back();
+        for (const PairDesc& d : descs)  // imaginary parts are accumulated with one observable group only
+            if (d.complex_out && nobs_max > 32)
+                raise(NSG_ERR_INVALID_ARGUMENT, nobs_max, 32, "complex pair sums take at most 32 observables per launch");
+        // One buffer: descriptors | desc_begin | obs_begin | row-chunk prefixes.
+        const size_t b_desc = sel.size() * sizeof(PairDesc);
+        const size_t b_db = dbegin.size() * 8, b_ob = obegin.size() * 8, b_off = offs.size() * 8;
+        keep_alive.emplace_back();
+        DBuf<unsigned char>& blob = keep_alive.back();
+        blob.alloc(b_desc + b_db + b_ob + b_off, st);
+        int64_t* d_db = (int64_t*)(blob.p + b_desc);
+        int64_t* d_ob = (int64_t*)(blob.p + b_desc + b_db);
+        int64_t* d_off = (int64_t*)(blob.p + b_desc + b_db + b_ob);
+        for (size_t q = 0; q < sel.size(); q++)
+            if (descs[q].triangular) descs[q].row_chunk_off = d_off + off_at[q];
+        std::vector<unsigned char> hb(b_desc + b_db + b_ob + b_off);
+        std::memcpy(hb.data(), descs.data(), b_desc);
+        std::memcpy(hb.data() + b_desc, dbegin.data(), b_db);
+        std::memcpy(hb.data() + b_desc + b_db, obegin.data(), b_ob);
+        if (b_off) std::memcpy(hb.data() + b_desc + b_db + b_ob, offs.data(), b_off);
+        CK(cudaMemcpyAsync(blob.p, hb.data(), hb.size(), cudaMemcpyHostToDevice, st));
+
+        MultiLaunch m;
+        m.descs = (const PairDesc*)blob.p;
+        m.num_descs = (int)sel.size();
+        m.desc_begin = d_db;
+        m.total_chunks = total;
+        m.chunk = kPairChunk;
+        m.nobs_max = nobs_max;
+        m.mixed = mixed;
+        const int wpb = 4;
+        const int64_t max_warps = (int64_t)sms * 16 * wpb;
+        m.per_warp = std::max<int64_t>(1, (total + max_warps - 1) / max_warps);
+        const int64_t warps = std::max<int64_t>(1, (total + m.per_warp - 1) / m.per_warp);
+        m.blocks = (int)((warps + wpb - 1) / wpb);
+        m.nwarps = m.blocks * wpb;
+        m.tab_bytes_max = tab_max;
+        m.warp_smem = pair_warp_smem_bytes(tab_max, wb);
+        if (sel.size() == 1) {
+            m.dbg_k = dbg_k;
+            m.dbg_r = dbg_r;
+        }
+        keep_rec.emplace_back();
+        DBuf<double>& rec = keep_rec.back();
+        rec.alloc((size_t)(m.nwarps + m.num_descs) * nobs_max * 8, st);
+        CK(cudaMemsetAsync(rec.p, 0, rec.n * sizeof(double), st));
+        m.records = rec.p;
+
+        cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+        if (prof) {
+            CK(cudaEventCreate(&ev0));
+            CK(cudaEventCreate(&ev1));
+            CK(cudaEventRecord(ev0, st));
+        }
+        CK(launch_pairs_multi(m, wb, st));
+        if (prof) {
+            CK(cudaEventRecord(ev1, st));
+            CK(cudaEventSynchronize(ev1));
+            float ms = 0.f;
+            CK(cudaEventElapsedTime(&ms, ev0, ev1));
+            cudaEventDestroy(ev0);
+            cudaEventDestroy(ev1);
+            prof_ms += ms;
+            prof_launches += 1;
+        }
+        DBuf<double> lout;
+        lout.alloc(2 * (size_t)obegin.back(), st);
+        CK(launch_reduce_multi(m, d_ob, obegin.back(), lout.p, st));
+        std::vector<double> hl(2 * (size_t)obegin.back());
+        CK(cudaMemcpyAsync(hl.data(), lout.p, hl.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        for (size_t q = 0; q < sel.size(); q++)
+            std::memcpy(hout.data() + 2 * unit_obs[sel[q]], hl.data() + 2 * obegin[q],
+                        2 * (size_t)live[sel[q]]->nobs * sizeof(double));
+    }
     if (prof) {
-        CK(cudaEventRecord(ev1, st));
-        CK(cudaEventSynchronize(ev1));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, ev0, ev1));
-        cudaEventDestroy(ev0);
-        cudaEventDestroy(ev1);
         std::lock_guard<std::mutex> lk(g_prof_mu);
-        g_prof_ms += ms;
-        g_prof_launches += 1;
-        g_prof_pairs += triangular ? (uint64_t)(chiA * (chiA + 1) / 2) : (uint64_t)(chiA * chiB);
+        g_prof_ms += prof_ms;
+        g_prof_launches += prof_launches;
+        g_prof_pairs += prof_pairs;
     }
-    double sre, sim;
-    if (complex_out) {  // conj(g_a)·g_b (stabilizer_decomposed_state/inner_product.rs:18)
-        sre = a->gf_re * b->gf_re + a->gf_im * b->gf_im;
-        sim = a->gf_re * b->gf_im - a->gf_im * b->gf_re;
-    } else {  // |g|² (exp_value.rs:60, norm.rs:29)
-        sre = a->gf_re * a->gf_re + a->gf_im * a->gf_im;
-        sim = 0.0;
+    CK(cudaStreamSynchronize(st));
+    for (size_t k = 0; k < live.size(); k++) {
+        PairUnit* u = live[k];
+        const double* r = hout.data() + 2 * unit_obs[k];
+        if (u->complex_out) {
+            std::memcpy(u->out, r, 2 * (size_t)u->nobs * sizeof(double));
+        } else {
+            for (int o = 0; o < u->nobs; o++) u->out[o] = r[2 * o];
+        }
     }
-    DBuf<double> dout;
-    dout.alloc(out.size(), st);
-    CK(launch_reduce(partials.p, pl.nwarps, nobs, complex_out, sre, sim, dout.p, st));
-    CK(cudaMemcpyAsync(out.data(), dout.p, out.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-    a->check_status();
+    // The launches ran on `st`; each bra state's status words report its units.
+    for (size_t k = 0; k < touched.size(); k++) touched[k]->check_status();
+}
+
+// Σ-pairs of one (a, b) for any number of observables (split into units of
+// at most 256), in one launch on a's stream.
+void run_pairs(nsg_state* a, nsg_state* b, const std::vector<DevPauli>& paulis, bool triangular, bool complex_out,
+               bool mixed, std::vector<double>& out, uint8_t* dbg_k = nullptr, int32_t* dbg_r = nullptr) {
+    const size_t nobs = paulis.size();
+    out.assign(complex_out ? 2 * nobs : nobs, 0.0);
+    std::vector<PairUnit> units;
+    for (size_t base = 0; base < nobs; base += kMaxObsPerUnit) {
+        PairUnit u;
+        u.a = a;
+        u.b = b;
+        u.paulis = paulis.data() + base;
+        u.nobs = (int)std::min<size_t>(kMaxObsPerUnit, nobs - base);
+        u.triangular = triangular;
+        u.complex_out = complex_out;
+        u.out = out.data() + (complex_out ? 2 * base : base);
+        units.push_back(u);
+    }
+    run_pair_units(units, mixed, a->st, units.size() == 1 ? dbg_k : nullptr, units.size() == 1 ? dbg_r : nullptr);
 }
 
 double norm_squared(nsg_state* s) {
@@ -975,14 +1132,9 @@ nsg_status nsg_exp_value_batch(const nsg_state* cstate, const nsg_pauli* paulis,
     require_pairs_width(state);
     std::vector<DevPauli> dp(num_paulis);
     for (size_t i = 0; i < num_paulis; i++) dp[i] = to_dev_pauli(paulis[i], state->t.n);
-    const size_t per = 256;  // observables per pass (8 lane groups)
-    for (size_t base = 0; base < num_paulis; base += per) {
-        size_t cnt = std::min(per, num_paulis - base);
-        std::vector<DevPauli> part(dp.begin() + base, dp.begin() + base + cnt);
-        std::vector<double> r;
-        run_pairs(state, state, part, true, false, precision == NSG_PRECISION_MIXED, r);
-        std::memcpy(out + base, r.data(), cnt * sizeof(double));
-    }
+    std::vector<double> r;
+    run_pairs(state, state, dp, true, false, precision == NSG_PRECISION_MIXED, r);
+    if (num_paulis) std::memcpy(out, r.data(), num_paulis * sizeof(double));
     API_END
 }
 
@@ -991,11 +1143,44 @@ nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states
     API_BEGIN
     need(pauli_offsets, "pauli_offsets");
     if (num_states) need(states, "states");
+    if (precision > NSG_PRECISION_MIXED) raise(NSG_ERR_INVALID_ARGUMENT, precision, -1, "invalid precision");
+    if (pauli_offsets[0] != 0) raise(NSG_ERR_INVALID_ARGUMENT, (int64_t)pauli_offsets[0], -1, "pauli_offsets[0] must be 0");
     for (size_t c = 0; c < num_states; c++) {
-        uint64_t b = pauli_offsets[c], e = pauli_offsets[c + 1];
-        if (e < b) raise(NSG_ERR_INVALID_ARGUMENT, (int64_t)c, -1, "pauli_offsets not ascending");
-        nsg_status rc = nsg_exp_value_batch(states[c], paulis + b, (size_t)(e - b), precision, out + b);
-        if (rc != NSG_OK) return rc;
+        need(states[c], "state");
+        if (pauli_offsets[c + 1] < pauli_offsets[c])
+            raise(NSG_ERR_INVALID_ARGUMENT, (int64_t)c, -1, "pauli_offsets not ascending at %zu", c);
+        require_pairs_width(states[c]);
+        if (states[c]->device != states[0]->device)
+            raise(NSG_ERR_INVALID_ARGUMENT, states[c]->device, states[0]->device, "all states must live on one device");
+    }
+    const uint64_t total = num_states ? pauli_offsets[num_states] : 0;
+    if (total) {
+        need(paulis, "paulis");
+        need(out, "out");
+    }
+    // Observables in device form, with the per-state length checks of exp_value.rs:9-27.
+    std::vector<DevPauli> dp(total);
+    for (size_t c = 0; c < num_states; c++)
+        for (uint64_t k = pauli_offsets[c]; k < pauli_offsets[c + 1]; k++)
+            dp[k] = to_dev_pauli(paulis[k], states[c]->t.n);
+    std::vector<PairUnit> units;
+    for (size_t c = 0; c < num_states; c++) {
+        nsg_state* s = const_cast<nsg_state*>(states[c]);
+        for (uint64_t base = pauli_offsets[c]; base < pauli_offsets[c + 1]; base += kMaxObsPerUnit) {
+            PairUnit u;
+            u.a = s;
+            u.b = s;
+            u.paulis = dp.data() + base;
+            u.nobs = (int)std::min<uint64_t>(kMaxObsPerUnit, pauli_offsets[c + 1] - base);
+            u.triangular = true;
+            u.complex_out = false;
+            u.out = out + base;
+            units.push_back(u);
+        }
+    }
+    if (!units.empty()) {
+        CK(cudaSetDevice(states[0]->device));
+        run_pair_units(units, precision == NSG_PRECISION_MIXED, const_cast<nsg_state*>(states[0])->st);
     }
     API_END
 }

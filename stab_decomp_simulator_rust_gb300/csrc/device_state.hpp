@@ -137,7 +137,55 @@ struct PairLaunch {
     int32_t* dbg_r = nullptr;
 };
 
-cudaError_t launch_pairs(const PairLaunch& p, cudaStream_t st);
+// One unit of a batched pair-sum launch: bra terms A (with their frames and
+// Pauli frames) against ket terms B (with their ket tables).
+struct PairDesc {
+    TermsView A;
+    TermsView B;
+    FrameView fr;                  // frames of A
+    const void* ktab = nullptr;    // ket tables of B
+    size_t ktab_stride = 0;
+    int ngrp = 0;
+    int nobs = 0;
+    const uint64_t* px = nullptr;  // [chiA][nobs] x_{A,P}
+    const uint8_t* pk = nullptr;   // [chiA][nobs] Z8 phase
+    int triangular = 1;            // exp_value/norm (A == B, i ≤ j) vs inner product (all pairs)
+    int complex_out = 0;
+    const int64_t* row_chunk_off = nullptr;  // triangular: [chiA+1] chunk prefix within the unit
+    int64_t cpr = 0;                         // rectangular: chunks per row
+    double scale_re = 1.0, scale_im = 0.0;   // |g|² or conj(g_a)·g_b
+    int* status = nullptr;                   // the owning state's status words
+};
+
+// A persistent launch over the concatenated chunk lists of many units; warp
+// w owns chunks [w·per_warp, (w+1)·per_warp) and accumulates into record
+// slot w + unit (deterministic; slots ≤ nwarps + num_descs).
+struct MultiLaunch {
+    const PairDesc* descs = nullptr;      // device [num_descs]
+    int num_descs = 0;
+    const int64_t* desc_begin = nullptr;  // device [num_descs+1] first global chunk of each unit
+    int64_t total_chunks = 0;
+    int64_t per_warp = 1;
+    int chunk = 32;
+    int nobs_max = 1;
+    bool mixed = false;
+    double* records = nullptr;            // [nwarps + num_descs][nobs_max][8]
+    int nwarps = 0;
+    int blocks = 0;
+    size_t tab_bytes_max = 0;             // largest ket_table_stride among the units
+    size_t warp_smem = 0;
+    uint8_t* dbg_k = nullptr;             // single-unit per-pair dump [chiA][chiB]
+    int32_t* dbg_r = nullptr;
+};
+
+// word_bytes: 4 when every unit of the launch has n ≤ 32, 8 when every unit
+// has 32 < n ≤ 64 (units are split by word width; ket tables are built with
+// the word width of their state, ket_table_stride).
+cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_t st);
+// out: 2 doubles (re, im) per observable, observables of unit u starting at obs_begin[u].
+cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, int64_t total_obs, double* out,
+                                cudaStream_t st);
+size_t pair_warp_smem_bytes(size_t tab_bytes_max, int word_bytes);
 
 // The same sums with B's rows staged per pair instead of ket tables (no
 // per-term table storage; at most 32 observables).
@@ -147,7 +195,6 @@ cudaError_t launch_pairs_rows(const PairLaunch& p, cudaStream_t st);
 // matrix P (n ≤ 64); sizes below.
 int ket_table_groups(int n);
 size_t ket_table_stride(int n);
-size_t pair_warp_smem(int n);
 cudaError_t launch_ket_tables(const TermsView& t, void* out, cudaStream_t st);
 
 // Reduce per-warp partials to one value (re, im) per observable, scaled by

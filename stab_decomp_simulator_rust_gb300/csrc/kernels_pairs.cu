@@ -440,16 +440,15 @@ __device__ __forceinline__ int nib(const Word x, int g) {  // 4-bit group g of a
 }
 
 template <typename Word, int RPL, int NG>
-__global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
+__global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
     constexpr int GMAX = (8 * sizeof(Word)) / 4;  // groups of four rows (8 or 16)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gwarp = blockIdx.x * PWARPS + wid;
     unsigned char* wbase = smem_raw + (size_t)wid * p.warp_smem;
-    const uint32_t tab_bytes = (uint32_t)p.ktab_stride;
     Word* tb0 = (Word*)wbase;
-    Word* tb1 = (Word*)(wbase + tab_bytes);
-    Word* sF = (Word*)(wbase + 2 * tab_bytes);
+    Word* tb1 = (Word*)(wbase + p.tab_bytes_max);
+    Word* sF = (Word*)(wbase + 2 * p.tab_bytes_max);
     Word* sM = sF + 64;
     uint64_t* bars = (uint64_t*)(sM + 64);
     if (lane == 0) {
@@ -459,13 +458,21 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
     }
     __syncwarp();
     uint32_t par0 = 0, par1 = 0;  // next phase parity per buffer
-    const unsigned char* ktab = (const unsigned char*)p.ktab;
 
-    const TermsView& A = p.A;
-    const TermsView& Bt = p.B;
-    const int n = A.n, ngrp = p.ngrp;
-    const int64_t chiA = A.chi, chiB = Bt.chi;
-    const int nobs = p.nobs;
+    // This warp's contiguous range of the global chunk list.
+    const int64_t c_begin = (int64_t)gwarp * p.per_warp;
+    const int64_t c_end = min(c_begin + p.per_warp, p.total_chunks);
+
+    // current descriptor
+    int ds = -1;
+    int64_t ds_end = 0;
+    const PairDesc* d = nullptr;
+    TermsView A, Bt;
+    const unsigned char* ktab = nullptr;
+    uint32_t tab_bytes = 0;
+    int n = 0, ngrp = 0, nobs = 0;
+    int64_t chiB = 0;
+    bool tri = true, cplx = false;
 
     int64_t cur_i = -1;
     Word GV[RPL], FV[RPL], MV[RPL];
@@ -474,36 +481,63 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
     int kcA = 0, rcA = 0;
     Word xs[NG];
     int ks[NG];
-    const int64_t cpr = p.triangular ? 0 : (chiB + p.chunk - 1) / p.chunk;
     int buf = 0;
     bool timed_out = false;
 
-    for (int64_t c = gwarp; c < p.total_chunks && !timed_out; c += p.nwarps) {
+    for (int64_t c = c_begin; c < c_end && !timed_out; c++) {
+        if (c >= ds_end) {  // enter the descriptor that owns chunk c
+            if (ds < 0) {
+                int lo = 0, hi = p.num_descs;
+                while (hi - lo > 1) {
+                    const int mid = (lo + hi) >> 1;
+                    if (p.desc_begin[mid] <= c) lo = mid;
+                    else hi = mid;
+                }
+                ds = lo;
+            } else {
+                while (p.desc_begin[ds + 1] <= c) ds++;
+            }
+            d = p.descs + ds;
+            ds_end = p.desc_begin[ds + 1];
+            A = d->A;
+            Bt = d->B;
+            ktab = (const unsigned char*)d->ktab;
+            tab_bytes = (uint32_t)d->ktab_stride;
+            n = A.n;
+            ngrp = d->ngrp;
+            nobs = d->nobs;
+            chiB = Bt.chi;
+            tri = d->triangular != 0;
+            cplx = d->complex_out != 0;
+            cur_i = -1;
+        }
+        const int64_t lc = c - p.desc_begin[ds];  // chunk index within the descriptor
         int64_t i, j0, j1;
-        if (p.triangular) {
-            int64_t lo = 0, hi = chiA;
+        if (tri) {
+            int64_t lo = 0, hi = A.chi;
             while (hi - lo > 1) {
                 int64_t mid = (lo + hi) >> 1;
-                if (p.row_chunk_off[mid] <= c) lo = mid;
+                if (d->row_chunk_off[mid] <= lc) lo = mid;
                 else hi = mid;
             }
             i = lo;
-            j0 = i + (c - p.row_chunk_off[i]) * p.chunk;
+            j0 = i + (lc - d->row_chunk_off[i]) * p.chunk;
         } else {
-            i = c / cpr;
-            j0 = (c % cpr) * p.chunk;
+            i = lc / d->cpr;
+            j0 = (lc % d->cpr) * p.chunk;
         }
         j1 = min(j0 + (int64_t)p.chunk, chiB);
         if (i != cur_i) {
             cur_i = i;
+            const FrameView& fr = d->fr;
 #pragma unroll
             for (int k = 0; k < RPL; k++) {
                 size_t o = (size_t)i * 64 + 32 * k + lane;
-                GV[k] = (Word)p.fr.GV[o];
-                FV[k] = (Word)p.fr.FV[o];
-                MV[k] = (Word)p.fr.MV[o];
+                GV[k] = (Word)fr.GV[o];
+                FV[k] = (Word)fr.FV[o];
+                MV[k] = (Word)fr.MV[o];
             }
-            const uint64_t gvl = p.fr.GVL[i], gvh = p.fr.GVH[i];
+            const uint64_t gvl = fr.GVL[i], gvh = fr.GVH[i];
             gamV = 0;
 #pragma unroll
             for (int k = 0; k < RPL; k++) {
@@ -517,10 +551,12 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
 #pragma unroll
             for (int g = 0; g < NG; g++) {
                 const int o = 32 * g + lane;
-                xs[g] = (o < nobs) ? (Word)p.px[(size_t)i * nobs + o] : (Word)0;
-                ks[g] = (o < nobs) ? p.pk[(size_t)i * nobs + o] : 0;
+                xs[g] = (o < nobs) ? (Word)d->px[(size_t)i * nobs + o] : (Word)0;
+                ks[g] = (o < nobs) ? d->pk[(size_t)i * nobs + o] : 0;
             }
         }
+        // this warp's partial record for the descriptor (slot gwarp + ds)
+        double* rec = p.records + (size_t)(gwarp + ds) * p.nobs_max * 8;
         constexpr int NA = (NG == 1) ? 4 : 2;
         ChunkAcc<NG, NA> acc;
         acc.reset();
@@ -551,7 +587,7 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
             if (!ok_wait) {
                 // Record the timeout, then give the prefetch into the other
                 // buffer (if one was issued) a bounded wait before leaving.
-                if (lane == 0) atomicOr(p.status, DS_TIMEOUT);
+                if (lane == 0) atomicOr(d->status, DS_TIMEOUT);
                 if (j + 1 < j1) {
                     if (buf) mbar_wait(&bars[0], par0);
                     else mbar_wait(&bars[1], par1);
@@ -602,11 +638,11 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
                 if (err && errq < 0) errq = q;
             }
             if (err && lane == 0) {
-                atomicOr(p.status, DS_INVARIANT);
-                if (atomicCAS(p.status + 1, 0, 1) == 0) {  // first hit: record where
-                    p.status[2] = (int)i;
-                    p.status[3] = (int)j;
-                    p.status[4] = errq;
+                atomicOr(d->status, DS_INVARIANT);
+                if (atomicCAS(d->status + 1, 0, 1) == 0) {  // first hit: record where
+                    d->status[2] = (int)i;
+                    d->status[3] = (int)j;
+                    d->status[4] = errq;
                 }
             }
 
@@ -646,7 +682,7 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
             }
             const int kpair = (kcB - kcA) & 7;
             const int rpair = rcA + rcB + rv;
-            const int wgt = (p.triangular && j != i) ? 2 : 1;
+            const int wgt = (tri && j != i) ? 2 : 1;
 #pragma unroll
             for (int g = 0; g < NG; g++) {
                 const int o = 32 * g + lane;
@@ -660,12 +696,12 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
                     p.dbg_r[di] = rv;
                 }
                 if (ok && o < nobs) {
-                    double* pp = p.partials + ((size_t)gwarp * nobs + o) * 8;
+                    double* pp = rec + (size_t)o * 8;
                     const int k = (kpair + ks[g] + kamp) & 7;
                     int sgn, m;
                     re_part(k, rpair, sgn, m);
                     if (sgn) acc.add(g, m & 1, sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1), p.mixed, pp);
-                    if (NA == 4 && p.complex_out) {
+                    if (NA == 4 && cplx) {
                         im_part(k, rpair, sgn, m);
                         if (sgn)
                             acc.add(g, (NA == 4 ? 2 : 0) + (m & 1), sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1),
@@ -676,12 +712,66 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(PairLaunch p) {
             __syncwarp();  // all lanes done with buffer `buf` and the staged rows
             buf ^= 1;
         }
-        // ---- flush the chunk into this warp's double-double partials
+        // ---- fold the chunk into this warp's double-double record
 #pragma unroll
         for (int g = 0; g < NG; g++) {
             const int o = 32 * g + lane;
-            if (o < nobs) acc.flush_group(g, p.partials + ((size_t)gwarp * nobs + o) * 8, p.mixed);
+            if (o < nobs) acc.flush_group(g, rec + (size_t)o * 8, p.mixed);
         }
+    }
+}
+
+// Reduction of the per-(warp, descriptor) records: one block per
+// (descriptor, observable), slots gwarp + ds over the warps whose chunk
+// ranges touch the descriptor, in a fixed double-double tree.
+__global__ void reduce_multi_kernel(MultiLaunch p, const int64_t* __restrict__ obs_begin, double* __restrict__ out) {
+    __shared__ double sh[8][256];
+    int lo = 0, hi = p.num_descs;  // descriptor of this block's observable
+    const int64_t ob = blockIdx.x;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (obs_begin[mid] <= ob) lo = mid;
+        else hi = mid;
+    }
+    const int ds = lo;
+    const PairDesc* d = p.descs + ds;
+    const int o = (int)(ob - obs_begin[ds]);
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const int64_t cb = p.desc_begin[ds], ce = p.desc_begin[ds + 1];
+    if (ce > cb) {
+        const int64_t w0 = cb / p.per_warp, w1 = (ce - 1) / p.per_warp;
+        for (int64_t w = w0 + threadIdx.x; w <= w1; w += blockDim.x) {
+            const double* pp = p.records + ((size_t)(w + ds) * p.nobs_max + o) * 8;
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                double s, e;
+                two_sum_d(acc[2 * t], pp[2 * t], s, e);
+                acc[2 * t] = s;
+                acc[2 * t + 1] += e + pp[2 * t + 1];
+            }
+        }
+    }
+#pragma unroll
+    for (int t = 0; t < 8; t++) sh[t][threadIdx.x] = acc[t];
+    __syncthreads();
+    for (int stride = blockDim.x / 2; stride > 0; stride >>= 1) {
+        if (threadIdx.x < stride) {
+#pragma unroll
+            for (int t = 0; t < 4; t++) {
+                double s, e;
+                two_sum_d(sh[2 * t][threadIdx.x], sh[2 * t][threadIdx.x + stride], s, e);
+                sh[2 * t][threadIdx.x] = s;
+                sh[2 * t + 1][threadIdx.x] += e + sh[2 * t + 1][threadIdx.x + stride];
+            }
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double r2 = 0.70710678118654752440;
+        const double re = (sh[0][0] + sh[1][0]) + (sh[2][0] + sh[3][0]) * r2;
+        const double im = (sh[4][0] + sh[5][0]) + (sh[6][0] + sh[7][0]) * r2;
+        out[2 * ob] = re * d->scale_re - im * d->scale_im;
+        out[2 * ob + 1] = re * d->scale_im + im * d->scale_re;
     }
 }
 
@@ -951,7 +1041,7 @@ __global__ void reduce_kernel(const double* __restrict__ partials, int nwarps, i
 }
 
 template <typename Word, int RPL, int NG>
-cudaError_t launch_pairs_ng(const PairLaunch& p, cudaStream_t st) {
+cudaError_t launch_pairs_ng(const MultiLaunch& p, cudaStream_t st) {
     const size_t smem = (size_t)p.warp_smem * PWARPS;
     static size_t configured = 0;  // per instantiation: raise the dynamic shared-memory limit once
     if (smem > 48 * 1024 && configured < smem) {
@@ -965,8 +1055,8 @@ cudaError_t launch_pairs_ng(const PairLaunch& p, cudaStream_t st) {
 }
 
 template <typename Word, int RPL>
-cudaError_t launch_pairs_w(const PairLaunch& p, cudaStream_t st) {
-    const int ng = (p.nobs + 31) / 32;
+cudaError_t launch_pairs_w(const MultiLaunch& p, cudaStream_t st) {
+    const int ng = (p.nobs_max + 31) / 32;
     if (ng <= 1) return launch_pairs_ng<Word, RPL, 1>(p, st);
     if (ng <= 2) return launch_pairs_ng<Word, RPL, 2>(p, st);
     if (ng <= 4) return launch_pairs_ng<Word, RPL, 4>(p, st);
@@ -1023,18 +1113,13 @@ cudaError_t launch_pauli_frames(const TermsView& t, const DevPauli* d_paulis, in
     return cudaGetLastError();
 }
 
-int pair_word_bytes(int n) { return n <= 32 ? 4 : 8; }
+static int pair_word_bytes(int n) { return n <= 32 ? 4 : 8; }
 
 size_t ket_table_stride(int n) {  // bytes per term: [4][ngrp][16] words
     return (size_t)4 * ket_table_groups(n) * 16 * pair_word_bytes(n);
 }
 
 int ket_table_groups(int n) { return n <= 0 ? 1 : (n + 3) / 4; }
-
-size_t pair_warp_smem(int n) {
-    size_t b = 2 * ket_table_stride(n) + 2 * 64 * (size_t)pair_word_bytes(n) + 2 * sizeof(uint64_t);
-    return (b + 127) & ~(size_t)127;
-}
 
 cudaError_t launch_ket_tables(const TermsView& t, void* out, cudaStream_t st) {
     if (t.chi == 0) return cudaSuccess;
@@ -1054,10 +1139,22 @@ cudaError_t launch_pairs_rows(const PairLaunch& p, cudaStream_t st) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_pairs(const PairLaunch& p, cudaStream_t st) {
-    if (p.total_chunks == 0) return cudaSuccess;
-    if (p.A.n <= 32) return launch_pairs_w<uint32_t, 1>(p, st);
-    return launch_pairs_w<uint64_t, 2>(p, st);
+cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_t st) {
+    if (m.total_chunks == 0) return cudaSuccess;
+    if (word_bytes == 4) return launch_pairs_w<uint32_t, 1>(m, st);
+    return launch_pairs_w<uint64_t, 2>(m, st);
+}
+
+cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, int64_t total_obs, double* out,
+                                cudaStream_t st) {
+    if (total_obs == 0) return cudaSuccess;
+    reduce_multi_kernel<<<(unsigned)total_obs, 256, 0, st>>>(m, obs_begin, out);
+    return cudaGetLastError();
+}
+
+size_t pair_warp_smem_bytes(size_t tab_bytes_max, int word_bytes) {
+    size_t b = 2 * tab_bytes_max + 2 * 64 * (size_t)word_bytes + 2 * sizeof(uint64_t);
+    return (b + 127) & ~(size_t)127;
 }
 
 cudaError_t launch_reduce(const double* partials, int nwarps, int nobs, bool complex_out, double scale_re,

@@ -237,3 +237,28 @@ class QuantumState:
         keys = ("G", "F", "M", "gamma", "v", "s", "phase", "coef_phase", "coef_r", "coef_zero", "global_factor")
         check(_ffi.load().nsg_export_terms(self._h, *[_p(d[k]) for k in keys]))
         return d
+
+
+def exp_values_multi(states, paulis_per_state, precision: int = PRECISION_FP64) -> list[np.ndarray]:
+    """⟨P⟩ for many states at once: observables ``paulis_per_state[c]`` on
+    ``states[c]``, every pair sum in one persistent launch (one per row width:
+    ≤ 32 and > 32 qubits).  Returns one array per state, each value as
+    ``states[c].exp_values(paulis_per_state[c], precision)`` gives it."""
+    states = list(states)
+    groups = [list(g) for g in paulis_per_state]
+    if len(groups) != len(states):
+        raise ValueError(f"got {len(states)} states but {len(groups)} observable lists")
+    offs = np.zeros(len(states) + 1, np.uint64)
+    for c, g in enumerate(groups):
+        offs[c + 1] = offs[c] + len(g)
+    total = int(offs[-1])
+    arr = (_ffi.PauliABI * max(total, 1))()
+    k = 0
+    for g in groups:
+        for p in g:
+            arr[k] = p.abi()
+            k += 1
+    hs = (C.c_void_p * max(len(states), 1))(*[s._h for s in states])
+    out = np.zeros(max(total, 1), np.float64)
+    check(_ffi.load().nsg_exp_value_multi(hs, len(states), arr, _p(offs), precision, _p(out)))
+    return [out[int(offs[c]):int(offs[c + 1])].copy() for c in range(len(states))]
