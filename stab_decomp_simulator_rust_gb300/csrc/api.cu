@@ -607,7 +607,6 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
         std::lock_guard<std::mutex> lk(g_prof_mu);
         prof = g_prof_on;
     }
-    const int sms = device_sm_count();
     std::vector<double> hout(2 * tot_obs, 0.0);
     std::vector<DBuf<unsigned char>> keep_alive;  // per-launch descriptor buffers
     std::vector<DBuf<double>> keep_rec;
@@ -632,7 +631,7 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
         if (sel.empty()) continue;
         // Host descriptors; row-chunk prefixes of the triangular units in one buffer.
         std::vector<PairDesc> descs(sel.size());
-        std::vector<int64_t> dbegin(sel.size() + 1, 0), obegin(sel.size() + 1, 0), offs;
+        std::vector<int64_t> tbegin(sel.size() + 1, 0), obegin(sel.size() + 1, 0), offs;
         std::vector<size_t> off_at(sel.size(), 0);
         size_t tab_max = 0;
         int nobs_max = 1;
@@ -675,18 +674,31 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
                 nch = chiA * d.cpr;
                 prof_pairs += (uint64_t)(chiA * chiB);
             }
-            dbegin[q + 1] = dbegin[q] + nch;
+            d.nchunks = nch;
             obegin[q + 1] = obegin[q] + u->nobs;
             tab_max = std::max(tab_max, d.ktab_stride);
             nobs_max = std::max(nobs_max, u->nobs);
         }
-        const int64_t total = dbegin.back();
         for (const PairDesc& d : descs)  // imaginary parts are accumulated with one observable group only
             if (d.complex_out && nobs_max > 32)
                 raise(NSG_ERR_INVALID_ARGUMENT, nobs_max, 32, "complex pair sums take at most 32 observables per launch");
-        // One buffer: descriptors | desc_begin | obs_begin | row-chunk prefixes.
+        // Tasks: about four per resident warp, never spanning two units.
+        const size_t warp_smem = pair_warp_smem_bytes(tab_max, wb);
+        const int64_t resident = pair_resident_warps(wb, nobs_max, warp_smem);
+        int64_t total_chunks = 0;
+        for (const PairDesc& d : descs) total_chunks += d.nchunks;
+        const int64_t task_chunks = std::max<int64_t>(1, (total_chunks + 4 * resident - 1) / (4 * resident));
+        int64_t rec_doubles = 0;
+        for (size_t q = 0; q < sel.size(); q++) {
+            const int64_t nt = (descs[q].nchunks + task_chunks - 1) / task_chunks;
+            tbegin[q + 1] = tbegin[q] + nt;
+            descs[q].rec0 = rec_doubles;
+            rec_doubles += nt * descs[q].nobs * 8;
+        }
+        const int64_t total_tasks = tbegin.back();
+        // One buffer: descriptors | task_begin | obs_begin | row-chunk prefixes.
         const size_t b_desc = sel.size() * sizeof(PairDesc);
-        const size_t b_db = dbegin.size() * 8, b_ob = obegin.size() * 8, b_off = offs.size() * 8;
+        const size_t b_db = tbegin.size() * 8, b_ob = obegin.size() * 8, b_off = offs.size() * 8;
         keep_alive.emplace_back();
         DBuf<unsigned char>& blob = keep_alive.back();
         blob.alloc(b_desc + b_db + b_ob + b_off, st);
@@ -697,7 +709,7 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
             if (descs[q].triangular) descs[q].row_chunk_off = d_off + off_at[q];
         std::vector<unsigned char> hb(b_desc + b_db + b_ob + b_off);
         std::memcpy(hb.data(), descs.data(), b_desc);
-        std::memcpy(hb.data() + b_desc, dbegin.data(), b_db);
+        std::memcpy(hb.data() + b_desc, tbegin.data(), b_db);
         std::memcpy(hb.data() + b_desc + b_db, obegin.data(), b_ob);
         if (b_off) std::memcpy(hb.data() + b_desc + b_db + b_ob, offs.data(), b_off);
         CK(cudaMemcpyAsync(blob.p, hb.data(), hb.size(), cudaMemcpyHostToDevice, st));
@@ -705,28 +717,28 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
         MultiLaunch m;
         m.descs = (const PairDesc*)blob.p;
         m.num_descs = (int)sel.size();
-        m.desc_begin = d_db;
-        m.total_chunks = total;
+        m.task_begin = d_db;
+        m.total_tasks = total_tasks;
+        m.task_chunks = (int)task_chunks;
         m.chunk = kPairChunk;
         m.nobs_max = nobs_max;
         m.mixed = mixed;
-        const int wpb = 4;
-        const int64_t max_warps = (int64_t)sms * 16 * wpb;
-        m.per_warp = std::max<int64_t>(1, (total + max_warps - 1) / max_warps);
-        const int64_t warps = std::max<int64_t>(1, (total + m.per_warp - 1) / m.per_warp);
-        m.blocks = (int)((warps + wpb - 1) / wpb);
+        const int wpb = 4;  // warps per block of the pair kernel
+        const int64_t warps = std::min<int64_t>(total_tasks, resident);
+        m.blocks = (int)std::max<int64_t>(1, (warps + wpb - 1) / wpb);
         m.nwarps = m.blocks * wpb;
         m.tab_bytes_max = tab_max;
-        m.warp_smem = pair_warp_smem_bytes(tab_max, wb);
+        m.warp_smem = warp_smem;
         if (sel.size() == 1) {
             m.dbg_k = dbg_k;
             m.dbg_r = dbg_r;
         }
         keep_rec.emplace_back();
         DBuf<double>& rec = keep_rec.back();
-        rec.alloc((size_t)(m.nwarps + m.num_descs) * nobs_max * 8, st);
+        rec.alloc((size_t)rec_doubles + 1, st);  // records, then the task counter
         CK(cudaMemsetAsync(rec.p, 0, rec.n * sizeof(double), st));
         m.records = rec.p;
+        m.counter = (unsigned long long*)(rec.p + rec_doubles);
 
         cudaEvent_t ev0 = nullptr, ev1 = nullptr;
         if (prof) {

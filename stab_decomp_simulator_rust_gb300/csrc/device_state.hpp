@@ -153,23 +153,28 @@ struct PairDesc {
     int complex_out = 0;
     const int64_t* row_chunk_off = nullptr;  // triangular: [chiA+1] chunk prefix within the unit
     int64_t cpr = 0;                         // rectangular: chunks per row
+    int64_t nchunks = 0;                     // chunks of the unit
+    int64_t rec0 = 0;                        // first double of the unit's task records
     double scale_re = 1.0, scale_im = 0.0;   // |g|² or conj(g_a)·g_b
     int* status = nullptr;                   // the owning state's status words
 };
 
-// A persistent launch over the concatenated chunk lists of many units; warp
-// w owns chunks [w·per_warp, (w+1)·per_warp) and accumulates into record
-// slot w + unit (deterministic; slots ≤ nwarps + num_descs).
+// A persistent launch over the task lists of many units.  Each unit's chunks
+// are cut into tasks of task_chunks chunks; warp w starts with task w and
+// takes further tasks from *counter.  Every task accumulates into its own
+// record ([nobs of its unit][8] doubles at rec0 + task·nobs·8), so the sums do
+// not depend on the schedule.
 struct MultiLaunch {
     const PairDesc* descs = nullptr;      // device [num_descs]
     int num_descs = 0;
-    const int64_t* desc_begin = nullptr;  // device [num_descs+1] first global chunk of each unit
-    int64_t total_chunks = 0;
-    int64_t per_warp = 1;
+    const int64_t* task_begin = nullptr;  // device [num_descs+1] first global task of each unit
+    int64_t total_tasks = 0;
+    int task_chunks = 1;
     int chunk = 32;
     int nobs_max = 1;
     bool mixed = false;
-    double* records = nullptr;            // [nwarps + num_descs][nobs_max][8]
+    double* records = nullptr;
+    unsigned long long* counter = nullptr;  // zero before the launch
     int nwarps = 0;
     int blocks = 0;
     size_t tab_bytes_max = 0;             // largest ket_table_stride among the units
@@ -186,6 +191,8 @@ cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_
 cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, int64_t total_obs, double* out,
                                 cudaStream_t st);
 size_t pair_warp_smem_bytes(size_t tab_bytes_max, int word_bytes);
+// Warps of the pair kernel resident on the whole device at once.
+int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem);
 
 // The same sums with B's rows staged per pair instead of ket tables (no
 // per-term table storage; at most 32 observables).

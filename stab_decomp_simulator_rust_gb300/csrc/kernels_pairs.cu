@@ -257,9 +257,20 @@ struct ChunkAcc {
 // Per term B: Four-Russians tables of its rows, 16 XOR combinations of each
 // group of four rows, for the matrices G, F, M and P, where P[q] holds the
 // bits r > q with parity(M_q·F_r) (so that Σ_{q<r∈f} M_q·F_r =
-// parity((f·P) ∧ f)).  Layout per term: [4][ngrp][16] Words.
+// parity((f·P) ∧ f)).  Layout per term: [4][ngrp][16] Words, then a
+// 48-byte trailer with the term's scalars (KetTrailer), so one bulk copy
+// brings everything the pair kernel reads of a ket.
+struct KetTrailer {
+    uint64_t gl, gh, v, s;  // γ planes, v, s (low word)
+    uint8_t phase, coef_k, pad0, pad1;
+    int32_t coef_r;
+    uint64_t pad2;
+};
+static_assert(sizeof(KetTrailer) == 48, "trailer size");
+
 template <typename Word>
-__global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, int ngrp, Word* __restrict__ out) {
+__global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, int ngrp, size_t stride,
+                                                                 unsigned char* __restrict__ out) {
     __shared__ Word sR[FWARPS][4][64];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t term = (int64_t)blockIdx.x * FWARPS + wid;
@@ -282,7 +293,7 @@ __global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, i
     }
     __syncwarp();
     const int per = ngrp * 16, total = 4 * per;
-    Word* dst = out + (size_t)term * total;
+    Word* dst = (Word*)(out + (size_t)term * stride);
     for (int e = lane; e < total; e += 32) {
         const int mat = e / per, g = (e / 16) % ngrp, idx = e & 15;
         Word acc = 0;
@@ -292,6 +303,19 @@ __global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, i
             if (((idx >> b) & 1) && row < n) acc ^= sR[wid][mat][row];
         }
         dst[e] = acc;
+    }
+    if (lane == 0) {
+        KetTrailer t;
+        t.gl = tv.GL[term * tv.W];
+        t.gh = tv.GH[term * tv.W];
+        t.v = tv.V[term * tv.W];
+        t.s = tv.S[term * tv.W];
+        t.phase = tv.phase[term];
+        t.coef_k = tv.coef_k[term];
+        t.pad0 = t.pad1 = 0;
+        t.coef_r = tv.coef_r[term];
+        t.pad2 = 0;
+        *(KetTrailer*)(dst + total) = t;
     }
 }
 
@@ -459,15 +483,9 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
     __syncwarp();
     uint32_t par0 = 0, par1 = 0;  // next phase parity per buffer
 
-    // This warp's contiguous range of the global chunk list.
-    const int64_t c_begin = (int64_t)gwarp * p.per_warp;
-    const int64_t c_end = min(c_begin + p.per_warp, p.total_chunks);
-
     // current descriptor
     int ds = -1;
-    int64_t ds_end = 0;
     const PairDesc* d = nullptr;
-    TermsView A, Bt;
     const unsigned char* ktab = nullptr;
     uint32_t tab_bytes = 0;
     int n = 0, ngrp = 0, nobs = 0;
@@ -484,246 +502,250 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
     int buf = 0;
     bool timed_out = false;
 
-    for (int64_t c = c_begin; c < c_end && !timed_out; c++) {
-        if (c >= ds_end) {  // enter the descriptor that owns chunk c
-            if (ds < 0) {
-                int lo = 0, hi = p.num_descs;
-                while (hi - lo > 1) {
-                    const int mid = (lo + hi) >> 1;
-                    if (p.desc_begin[mid] <= c) lo = mid;
-                    else hi = mid;
-                }
-                ds = lo;
-            } else {
-                while (p.desc_begin[ds + 1] <= c) ds++;
+    // Work queue: the first task of every warp is its own index, the next
+    // ones come from a global counter.  A task is a run of at most
+    // task_chunks chunks inside one descriptor and owns one record (so the
+    // sums do not depend on which warp ran which task).
+    int64_t task = gwarp;
+    while (task < p.total_tasks && !timed_out) {
+        if (ds < 0 || task >= p.task_begin[ds + 1]) {  // enter the descriptor that owns the task
+            int lo = ds < 0 ? 0 : ds, hi = p.num_descs;
+            while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (p.task_begin[mid] <= task) lo = mid;
+                else hi = mid;
             }
+            ds = lo;
             d = p.descs + ds;
-            ds_end = p.desc_begin[ds + 1];
-            A = d->A;
-            Bt = d->B;
             ktab = (const unsigned char*)d->ktab;
             tab_bytes = (uint32_t)d->ktab_stride;
-            n = A.n;
+            n = d->A.n;
             ngrp = d->ngrp;
             nobs = d->nobs;
-            chiB = Bt.chi;
+            chiB = d->B.chi;
             tri = d->triangular != 0;
             cplx = d->complex_out != 0;
             cur_i = -1;
         }
-        const int64_t lc = c - p.desc_begin[ds];  // chunk index within the descriptor
-        int64_t i, j0, j1;
-        if (tri) {
-            int64_t lo = 0, hi = A.chi;
-            while (hi - lo > 1) {
-                int64_t mid = (lo + hi) >> 1;
-                if (d->row_chunk_off[mid] <= lc) lo = mid;
-                else hi = mid;
-            }
-            i = lo;
-            j0 = i + (lc - d->row_chunk_off[i]) * p.chunk;
-        } else {
-            i = lc / d->cpr;
-            j0 = (lc % d->cpr) * p.chunk;
-        }
-        j1 = min(j0 + (int64_t)p.chunk, chiB);
-        if (i != cur_i) {
-            cur_i = i;
-            const FrameView& fr = d->fr;
-#pragma unroll
-            for (int k = 0; k < RPL; k++) {
-                size_t o = (size_t)i * 64 + 32 * k + lane;
-                GV[k] = (Word)fr.GV[o];
-                FV[k] = (Word)fr.FV[o];
-                MV[k] = (Word)fr.MV[o];
-            }
-            const uint64_t gvl = fr.GVL[i], gvh = fr.GVH[i];
-            gamV = 0;
-#pragma unroll
-            for (int k = 0; k < RPL; k++) {
-                const int r = 32 * k + lane;
-                gamV |= (uint32_t)(((gvl >> r) & 1) | (((gvh >> r) & 1) << 1)) << (2 * k);
-            }
-            vA = (Word)A.V[i * A.W];
-            sA = (Word)A.S[i * A.W];
-            kcA = A.coef_k[i];
-            rcA = A.coef_r[i];
-#pragma unroll
-            for (int g = 0; g < NG; g++) {
-                const int o = 32 * g + lane;
-                xs[g] = (o < nobs) ? (Word)d->px[(size_t)i * nobs + o] : (Word)0;
-                ks[g] = (o < nobs) ? d->pk[(size_t)i * nobs + o] : 0;
-            }
-        }
-        // this warp's partial record for the descriptor (slot gwarp + ds)
-        double* rec = p.records + (size_t)(gwarp + ds) * p.nobs_max * 8;
-        constexpr int NA = (NG == 1) ? 4 : 2;
-        ChunkAcc<NG, NA> acc;
-        acc.reset();
-
-        // first ket of the chunk
-        if (lane == 0) {
-            fence_proxy_async();
-            tma_load(buf ? tb1 : tb0, ktab + (size_t)j0 * tab_bytes, tab_bytes, buf ? &bars[1] : &bars[0]);
-        }
-        for (int64_t j = j0; j < j1; j++) {
-            // prefetch the next ket's tables into the other buffer
-            if (j + 1 < j1 && lane == 0) {
-                fence_proxy_async();
-                tma_load(buf ? tb0 : tb1, ktab + (size_t)(j + 1) * tab_bytes, tab_bytes, buf ? &bars[0] : &bars[1]);
-            }
-            const Word glB = (Word)Bt.GL[j * Bt.W], ghB = (Word)Bt.GH[j * Bt.W];
-            Word v = (Word)Bt.V[j * Bt.W], s = (Word)Bt.S[j * Bt.W];
-            int phase = Bt.phase[j];
-            const int kcB = Bt.coef_k[j], rcB = Bt.coef_r[j];
-            bool ok_wait;
-            if (buf) {
-                ok_wait = mbar_wait(&bars[1], par1);
-                par1 ^= 1;
+        const int64_t tl = task - p.task_begin[ds];
+        const int64_t c0 = tl * p.task_chunks, c1 = min(c0 + (int64_t)p.task_chunks, d->nchunks);
+        double* rec = p.records + d->rec0 + tl * (int64_t)nobs * 8;  // this task's record
+        for (int64_t lc = c0; lc < c1 && !timed_out; lc++) {
+            int64_t i, j0, j1;
+            if (tri) {
+                int64_t lo = 0, hi = d->A.chi;
+                while (hi - lo > 1) {
+                    int64_t mid = (lo + hi) >> 1;
+                    if (d->row_chunk_off[mid] <= lc) lo = mid;
+                    else hi = mid;
+                }
+                i = lo;
+                j0 = i + (lc - d->row_chunk_off[i]) * p.chunk;
             } else {
-                ok_wait = mbar_wait(&bars[0], par0);
-                par0 ^= 1;
+                i = lc / d->cpr;
+                j0 = (lc % d->cpr) * p.chunk;
             }
-            if (!ok_wait) {
-                // Record the timeout, then give the prefetch into the other
-                // buffer (if one was issued) a bounded wait before leaving.
-                if (lane == 0) atomicOr(d->status, DS_TIMEOUT);
-                if (j + 1 < j1) {
-                    if (buf) mbar_wait(&bars[0], par0);
-                    else mbar_wait(&bars[1], par1);
+            j1 = min(j0 + (int64_t)p.chunk, chiB);
+            if (i != cur_i) {
+                cur_i = i;
+                const FrameView& fr = d->fr;
+#pragma unroll
+                for (int k = 0; k < RPL; k++) {
+                    size_t o = (size_t)i * 64 + 32 * k + lane;
+                    GV[k] = (Word)fr.GV[o];
+                    FV[k] = (Word)fr.FV[o];
+                    MV[k] = (Word)fr.MV[o];
                 }
-                timed_out = true;
-                break;
-            }
-            const Word* T = buf ? tb1 : tb0;
-
-            // ---- D = V·U_B by table lookups (Four Russians)
-            Word gD[RPL], fD[RPL], mD[RPL], y[RPL];
+                const uint64_t gvl = fr.GVL[i], gvh = fr.GVH[i];
+                gamV = 0;
 #pragma unroll
-            for (int k = 0; k < RPL; k++) gD[k] = fD[k] = mD[k] = y[k] = 0;
-#pragma unroll
-            for (int g = 0; g < GMAX; g++) {
-                if (g < ngrp) {
-                    const Word* TG = T + g * 16;
-                    const Word* TF = T + (ngrp + g) * 16;
-                    const Word* TM = T + (2 * ngrp + g) * 16;
-                    const Word* TP = T + (3 * ngrp + g) * 16;
-#pragma unroll
-                    for (int k = 0; k < RPL; k++) {
-                        const int ig = nib<Word, RPL>(GV[k], g), jf = nib<Word, RPL>(FV[k], g),
-                                  im = nib<Word, RPL>(MV[k], g);
-                        gD[k] ^= TG[ig];
-                        fD[k] ^= TF[jf];
-                        mD[k] ^= TM[jf] ^ TG[im];
-                        y[k] ^= TP[jf];
-                    }
+                for (int k = 0; k < RPL; k++) {
+                    const int r = 32 * k + lane;
+                    gamV |= (uint32_t)(((gvl >> r) & 1) | (((gvh >> r) & 1) << 1)) << (2 * k);
                 }
-            }
-            uint32_t gam = 0;
-#pragma unroll
-            for (int k = 0; k < RPL; k++) {
-                const int gsum = popc<Word>(FV[k] & glB) + 2 * popc<Word>(FV[k] & ghB);
-                const int g = (int)((gamV >> (2 * k)) & 3) + gsum + 2 * parity<Word>(y[k] & FV[k]);
-                gam |= (uint32_t)(g & 3) << (2 * k);
-            }
-
-            // ---- U_{H,A}
-            int err = 0;
-            Word hv = vA;
-            int errq = -1;
-            while (hv) {
-                const int q = ffs0<Word>(hv);
-                hv &= hv - 1;
-                pair_h<Word, RPL>(gD, fD, mD, gam, v, s, phase, q, err);
-                if (err && errq < 0) errq = q;
-            }
-            if (err && lane == 0) {
-                atomicOr(d->status, DS_INVARIANT);
-                if (atomicCAS(d->status + 1, 0, 1) == 0) {  // first hit: record where
-                    d->status[2] = (int)i;
-                    d->status[3] = (int)j;
-                    d->status[4] = errq;
-                }
-            }
-
-            // ---- stage F, M rows of the transformed ket; γ planes by ballot
-#pragma unroll
-            for (int k = 0; k < RPL; k++) {
-                sF[32 * k + lane] = fD[k];
-                sM[32 * k + lane] = mD[k];
-            }
-            Word gl2 = 0, gh2 = 0;
-#pragma unroll
-            for (int k = 0; k < RPL; k++) {
-                const uint32_t b0 = __ballot_sync(FULL, gam & (1u << (2 * k)));
-                const uint32_t b1 = __ballot_sync(FULL, gam & (2u << (2 * k)));
-                gl2 |= (Word)b0 << (32 * k);
-                gh2 |= (Word)b1 << (32 * k);
-            }
-            __syncwarp();
-            const int rv = popc<Word>(v);
-
-            // ---- amplitudes ⟨x|ket⟩: u = xF, m = xM, ordered sign Σ_{p<r∈x} M_p·F_r
-            //      (parity accumulated as an XOR of the masked products).
-            Word u[NG], mac[NG], sacc[NG];
-#pragma unroll
-            for (int g = 0; g < NG; g++) u[g] = mac[g] = sacc[g] = 0;
-            for (int q = 0; q < n; q++) {
-                const Word f = sF[q], m = sM[q];
-                const Word bit = (Word)1 << q;
+                const TermsView& A = d->A;
+                vA = (Word)A.V[i * A.W];
+                sA = (Word)A.S[i * A.W];
+                kcA = A.coef_k[i];
+                rcA = A.coef_r[i];
 #pragma unroll
                 for (int g = 0; g < NG; g++) {
-                    const Word sel = (xs[g] & bit) ? ~(Word)0 : (Word)0;
-                    const Word fs = f & sel;
-                    sacc[g] ^= mac[g] & fs;
-                    mac[g] ^= m & sel;
-                    u[g] ^= fs;
+                    const int o = 32 * g + lane;
+                    xs[g] = (o < nobs) ? (Word)d->px[(size_t)i * nobs + o] : (Word)0;
+                    ks[g] = (o < nobs) ? d->pk[(size_t)i * nobs + o] : 0;
                 }
             }
-            const int kpair = (kcB - kcA) & 7;
-            const int rpair = rcA + rcB + rv;
-            const int wgt = (tri && j != i) ? 2 : 1;
+            constexpr int NA = (NG == 1) ? 4 : 2;
+            ChunkAcc<NG, NA> acc;
+            acc.reset();
+
+            // first ket of the chunk
+            if (lane == 0) {
+                fence_proxy_async();
+                tma_load(buf ? tb1 : tb0, ktab + (size_t)j0 * tab_bytes, tab_bytes, buf ? &bars[1] : &bars[0]);
+            }
+            for (int64_t j = j0; j < j1; j++) {
+                // prefetch the next ket's tables into the other buffer
+                if (j + 1 < j1 && lane == 0) {
+                    fence_proxy_async();
+                    tma_load(buf ? tb0 : tb1, ktab + (size_t)(j + 1) * tab_bytes, tab_bytes, buf ? &bars[0] : &bars[1]);
+                }
+                bool ok_wait;
+                if (buf) {
+                    ok_wait = mbar_wait(&bars[1], par1);
+                    par1 ^= 1;
+                } else {
+                    ok_wait = mbar_wait(&bars[0], par0);
+                    par0 ^= 1;
+                }
+                if (!ok_wait) {
+                    // Record the timeout, then give the prefetch into the other
+                    // buffer (if one was issued) a bounded wait before leaving.
+                    if (lane == 0) atomicOr(d->status, DS_TIMEOUT);
+                    if (j + 1 < j1) {
+                        if (buf) mbar_wait(&bars[0], par0);
+                        else mbar_wait(&bars[1], par1);
+                    }
+                    timed_out = true;
+                    break;
+                }
+                const Word* T = buf ? tb1 : tb0;
+                const KetTrailer& kt = *(const KetTrailer*)(T + 4 * ngrp * 16);  // the ket's scalars
+                const Word glB = (Word)kt.gl, ghB = (Word)kt.gh;
+                Word v = (Word)kt.v, s = (Word)kt.s;
+                int phase = kt.phase;
+                const int kcB = kt.coef_k, rcB = kt.coef_r;
+
+                // ---- D = V·U_B by table lookups (Four Russians)
+                Word gD[RPL], fD[RPL], mD[RPL], y[RPL];
+#pragma unroll
+                for (int k = 0; k < RPL; k++) gD[k] = fD[k] = mD[k] = y[k] = 0;
+#pragma unroll
+                for (int g = 0; g < GMAX; g++) {
+                    if (g < ngrp) {
+                        const Word* TG = T + g * 16;
+                        const Word* TF = T + (ngrp + g) * 16;
+                        const Word* TM = T + (2 * ngrp + g) * 16;
+                        const Word* TP = T + (3 * ngrp + g) * 16;
+#pragma unroll
+                        for (int k = 0; k < RPL; k++) {
+                            const int ig = nib<Word, RPL>(GV[k], g), jf = nib<Word, RPL>(FV[k], g),
+                                      im = nib<Word, RPL>(MV[k], g);
+                            gD[k] ^= TG[ig];
+                            fD[k] ^= TF[jf];
+                            mD[k] ^= TM[jf] ^ TG[im];
+                            y[k] ^= TP[jf];
+                        }
+                    }
+                }
+                uint32_t gam = 0;
+#pragma unroll
+                for (int k = 0; k < RPL; k++) {
+                    const int gsum = popc<Word>(FV[k] & glB) + 2 * popc<Word>(FV[k] & ghB);
+                    const int g = (int)((gamV >> (2 * k)) & 3) + gsum + 2 * parity<Word>(y[k] & FV[k]);
+                    gam |= (uint32_t)(g & 3) << (2 * k);
+                }
+
+                // ---- U_{H,A}
+                int err = 0;
+                Word hv = vA;
+                int errq = -1;
+                while (hv) {
+                    const int q = ffs0<Word>(hv);
+                    hv &= hv - 1;
+                    pair_h<Word, RPL>(gD, fD, mD, gam, v, s, phase, q, err);
+                    if (err && errq < 0) errq = q;
+                }
+                if (err && lane == 0) {
+                    atomicOr(d->status, DS_INVARIANT);
+                    if (atomicCAS(d->status + 1, 0, 1) == 0) {  // first hit: record where
+                        d->status[2] = (int)i;
+                        d->status[3] = (int)j;
+                        d->status[4] = errq;
+                    }
+                }
+
+                // ---- stage F, M rows of the transformed ket; γ planes by ballot
+#pragma unroll
+                for (int k = 0; k < RPL; k++) {
+                    sF[32 * k + lane] = fD[k];
+                    sM[32 * k + lane] = mD[k];
+                }
+                Word gl2 = 0, gh2 = 0;
+#pragma unroll
+                for (int k = 0; k < RPL; k++) {
+                    const uint32_t b0 = __ballot_sync(FULL, gam & (1u << (2 * k)));
+                    const uint32_t b1 = __ballot_sync(FULL, gam & (2u << (2 * k)));
+                    gl2 |= (Word)b0 << (32 * k);
+                    gh2 |= (Word)b1 << (32 * k);
+                }
+                __syncwarp();
+                const int rv = popc<Word>(v);
+
+                // ---- amplitudes ⟨x|ket⟩: u = xF, m = xM, ordered sign Σ_{p<r∈x} M_p·F_r
+                //      (parity accumulated as an XOR of the masked products).
+                Word u[NG], mac[NG], sacc[NG];
+#pragma unroll
+                for (int g = 0; g < NG; g++) u[g] = mac[g] = sacc[g] = 0;
+                for (int q = 0; q < n; q++) {
+                    const Word f = sF[q], m = sM[q];
+                    const Word bit = (Word)1 << q;
+#pragma unroll
+                    for (int g = 0; g < NG; g++) {
+                        const Word sel = (xs[g] & bit) ? ~(Word)0 : (Word)0;
+                        const Word fs = f & sel;
+                        sacc[g] ^= mac[g] & fs;
+                        mac[g] ^= m & sel;
+                        u[g] ^= fs;
+                    }
+                }
+                const int kpair = (kcB - kcA) & 7;
+                const int rpair = rcA + rcB + rv;
+                const int wgt = (tri && j != i) ? 2 : 1;
+#pragma unroll
+                for (int g = 0; g < NG; g++) {
+                    const int o = 32 * g + lane;
+                    const bool ok = (((u[g] ^ s) & ~v) == 0);
+                    const int gsum = popc<Word>(xs[g] & gl2) + 2 * popc<Word>(xs[g] & gh2);
+                    const int sg = parity<Word>(sacc[g] ^ (u[g] & mac[g]) ^ (u[g] & v & s));
+                    const int kamp = (phase + 2 * gsum + 4 * sg) & 7;
+                    if (p.dbg_k && o == 0) {
+                        const size_t di = (size_t)i * chiB + j;
+                        p.dbg_k[di] = ok ? (uint8_t)((ks[g] + kamp) & 7) : (uint8_t)255;
+                        p.dbg_r[di] = rv;
+                    }
+                    if (ok && o < nobs) {
+                        double* pp = rec + (size_t)o * 8;
+                        const int k = (kpair + ks[g] + kamp) & 7;
+                        int sgn, m;
+                        re_part(k, rpair, sgn, m);
+                        if (sgn) acc.add(g, m & 1, sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1), p.mixed, pp);
+                        if (NA == 4 && cplx) {
+                            im_part(k, rpair, sgn, m);
+                            if (sgn)
+                                acc.add(g, (NA == 4 ? 2 : 0) + (m & 1), sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1),
+                                        p.mixed, pp);
+                        }
+                    }
+                }
+                __syncwarp();  // all lanes done with buffer `buf` and the staged rows
+                buf ^= 1;
+            }
+            // ---- fold the chunk into the task's double-double record
 #pragma unroll
             for (int g = 0; g < NG; g++) {
                 const int o = 32 * g + lane;
-                const bool ok = (((u[g] ^ s) & ~v) == 0);
-                const int gsum = popc<Word>(xs[g] & gl2) + 2 * popc<Word>(xs[g] & gh2);
-                const int sg = parity<Word>(sacc[g] ^ (u[g] & mac[g]) ^ (u[g] & v & s));
-                const int kamp = (phase + 2 * gsum + 4 * sg) & 7;
-                if (p.dbg_k && o == 0) {
-                    const size_t di = (size_t)i * chiB + j;
-                    p.dbg_k[di] = ok ? (uint8_t)((ks[g] + kamp) & 7) : (uint8_t)255;
-                    p.dbg_r[di] = rv;
-                }
-                if (ok && o < nobs) {
-                    double* pp = rec + (size_t)o * 8;
-                    const int k = (kpair + ks[g] + kamp) & 7;
-                    int sgn, m;
-                    re_part(k, rpair, sgn, m);
-                    if (sgn) acc.add(g, m & 1, sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1), p.mixed, pp);
-                    if (NA == 4 && cplx) {
-                        im_part(k, rpair, sgn, m);
-                        if (sgn)
-                            acc.add(g, (NA == 4 ? 2 : 0) + (m & 1), sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1),
-                                    p.mixed, pp);
-                    }
-                }
+                if (o < nobs) acc.flush_group(g, rec + (size_t)o * 8, p.mixed);
             }
-            __syncwarp();  // all lanes done with buffer `buf` and the staged rows
-            buf ^= 1;
         }
-        // ---- fold the chunk into this warp's double-double record
-#pragma unroll
-        for (int g = 0; g < NG; g++) {
-            const int o = 32 * g + lane;
-            if (o < nobs) acc.flush_group(g, rec + (size_t)o * 8, p.mixed);
-        }
+        unsigned long long next = 0;
+        if (lane == 0) next = atomicAdd(p.counter, 1ULL);
+        task = (int64_t)shfl<unsigned long long>(next, 0) + p.nwarps;
     }
 }
 
-// Reduction of the per-(warp, descriptor) records: one block per
-// (descriptor, observable), slots gwarp + ds over the warps whose chunk
-// ranges touch the descriptor, in a fixed double-double tree.
+// Reduction of the per-task records: one block per (descriptor,
+// observable) over the descriptor's tasks, in a fixed double-double tree.
 __global__ void reduce_multi_kernel(MultiLaunch p, const int64_t* __restrict__ obs_begin, double* __restrict__ out) {
     __shared__ double sh[8][256];
     int lo = 0, hi = p.num_descs;  // descriptor of this block's observable
@@ -737,11 +759,10 @@ __global__ void reduce_multi_kernel(MultiLaunch p, const int64_t* __restrict__ o
     const PairDesc* d = p.descs + ds;
     const int o = (int)(ob - obs_begin[ds]);
     double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int64_t cb = p.desc_begin[ds], ce = p.desc_begin[ds + 1];
-    if (ce > cb) {
-        const int64_t w0 = cb / p.per_warp, w1 = (ce - 1) / p.per_warp;
-        for (int64_t w = w0 + threadIdx.x; w <= w1; w += blockDim.x) {
-            const double* pp = p.records + ((size_t)(w + ds) * p.nobs_max + o) * 8;
+    const int64_t ntasks = p.task_begin[ds + 1] - p.task_begin[ds];
+    {
+        for (int64_t tl = threadIdx.x; tl < ntasks; tl += blockDim.x) {
+            const double* pp = p.records + d->rec0 + (tl * d->nobs + o) * 8;
 #pragma unroll
             for (int t = 0; t < 4; t++) {
                 double s, e;
@@ -1040,18 +1061,39 @@ __global__ void reduce_kernel(const double* __restrict__ partials, int nwarps, i
     }
 }
 
+// Dynamic shared memory above 48 KB needs an opt-in per kernel (and device).
+template <typename Word, int RPL, int NG>
+cudaError_t allow_smem(size_t smem) {
+    if (smem <= 48 * 1024) return cudaSuccess;
+    return cudaFuncSetAttribute(pair_kernel<Word, RPL, NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 template <typename Word, int RPL, int NG>
 cudaError_t launch_pairs_ng(const MultiLaunch& p, cudaStream_t st) {
     const size_t smem = (size_t)p.warp_smem * PWARPS;
-    static size_t configured = 0;  // per instantiation: raise the dynamic shared-memory limit once
-    if (smem > 48 * 1024 && configured < smem) {
-        cudaError_t e = cudaFuncSetAttribute(pair_kernel<Word, RPL, NG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = smem;
-    }
+    cudaError_t e = allow_smem<Word, RPL, NG>(smem);
+    if (e != cudaSuccess) return e;
     pair_kernel<Word, RPL, NG><<<p.blocks, PWARPS * 32, smem, st>>>(p);
     return cudaGetLastError();
+}
+
+template <typename Word, int RPL, int NG>
+int resident_blocks_ng(size_t warp_smem) {
+    int nb = 0;
+    if (allow_smem<Word, RPL, NG>(warp_smem * PWARPS) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pair_kernel<Word, RPL, NG>, PWARPS * 32,
+                                                      warp_smem * PWARPS) != cudaSuccess)
+        return 1;
+    return nb > 0 ? nb : 1;
+}
+
+template <typename Word, int RPL>
+int resident_blocks_w(int nobs_max, size_t warp_smem) {
+    const int ng = (nobs_max + 31) / 32;
+    if (ng <= 1) return resident_blocks_ng<Word, RPL, 1>(warp_smem);
+    if (ng <= 2) return resident_blocks_ng<Word, RPL, 2>(warp_smem);
+    if (ng <= 4) return resident_blocks_ng<Word, RPL, 4>(warp_smem);
+    return resident_blocks_ng<Word, RPL, 8>(warp_smem);
 }
 
 template <typename Word, int RPL>
@@ -1115,8 +1157,8 @@ cudaError_t launch_pauli_frames(const TermsView& t, const DevPauli* d_paulis, in
 
 static int pair_word_bytes(int n) { return n <= 32 ? 4 : 8; }
 
-size_t ket_table_stride(int n) {  // bytes per term: [4][ngrp][16] words
-    return (size_t)4 * ket_table_groups(n) * 16 * pair_word_bytes(n);
+size_t ket_table_stride(int n) {  // bytes per term: [4][ngrp][16] words + trailer
+    return (size_t)4 * ket_table_groups(n) * 16 * pair_word_bytes(n) + sizeof(KetTrailer);
 }
 
 int ket_table_groups(int n) { return n <= 0 ? 1 : (n + 3) / 4; }
@@ -1125,9 +1167,11 @@ cudaError_t launch_ket_tables(const TermsView& t, void* out, cudaStream_t st) {
     if (t.chi == 0) return cudaSuccess;
     const unsigned blocks = (unsigned)((t.chi + FWARPS - 1) / FWARPS);
     if (t.n <= 32)
-        ket_tables_kernel<uint32_t><<<blocks, FWARPS * 32, 0, st>>>(t, ket_table_groups(t.n), (uint32_t*)out);
+        ket_tables_kernel<uint32_t><<<blocks, FWARPS * 32, 0, st>>>(t, ket_table_groups(t.n), ket_table_stride(t.n),
+                                                                    (unsigned char*)out);
     else
-        ket_tables_kernel<uint64_t><<<blocks, FWARPS * 32, 0, st>>>(t, ket_table_groups(t.n), (uint64_t*)out);
+        ket_tables_kernel<uint64_t><<<blocks, FWARPS * 32, 0, st>>>(t, ket_table_groups(t.n), ket_table_stride(t.n),
+                                                                    (unsigned char*)out);
     return cudaGetLastError();
 }
 
@@ -1140,9 +1184,15 @@ cudaError_t launch_pairs_rows(const PairLaunch& p, cudaStream_t st) {
 }
 
 cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_t st) {
-    if (m.total_chunks == 0) return cudaSuccess;
+    if (m.total_tasks == 0) return cudaSuccess;
     if (word_bytes == 4) return launch_pairs_w<uint32_t, 1>(m, st);
     return launch_pairs_w<uint64_t, 2>(m, st);
+}
+
+int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem) {
+    const int nb = word_bytes == 4 ? resident_blocks_w<uint32_t, 1>(nobs_max, warp_smem)
+                                   : resident_blocks_w<uint64_t, 2>(nobs_max, warp_smem);
+    return nb * PWARPS * device_sm_count();
 }
 
 cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, int64_t total_obs, double* out,
