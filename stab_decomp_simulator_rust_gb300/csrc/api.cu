@@ -577,6 +577,7 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
     std::vector<nsg_state*> touched;
     for (PairUnit* u : live) {
         u->a->frames();
+        u->a->ket_tables();
         u->b->ket_tables();
         touched.push_back(u->a);
         touched.push_back(u->b);
@@ -633,7 +634,7 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
         std::vector<PairDesc> descs(sel.size());
         std::vector<int64_t> tbegin(sel.size() + 1, 0), obegin(sel.size() + 1, 0), offs;
         std::vector<size_t> off_at(sel.size(), 0);
-        size_t tab_max = 0;
+        size_t tab_max = 0, bra_max = 0;
         int nobs_max = 1;
         for (size_t q = 0; q < sel.size(); q++) {
             PairUnit* u = live[sel[q]];
@@ -643,7 +644,9 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
             d.B = u->b->t.view();
             d.fr = u->a->frames();
             d.ktab = u->b->ket_tables();
+            d.atab = u->a->ket_tables();
             d.ktab_stride = ket_table_stride(u->b->t.n);
+            d.ket_bytes = (uint32_t)ket_table_ket_bytes(u->b->t.n);
             d.ngrp = ket_table_groups(u->b->t.n);
             d.nobs = u->nobs;
             d.px = px.p + unit_px[sel[q]];
@@ -676,14 +679,15 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
             }
             d.nchunks = nch;
             obegin[q + 1] = obegin[q] + u->nobs;
-            tab_max = std::max(tab_max, d.ktab_stride);
+            tab_max = std::max(tab_max, (size_t)d.ket_bytes);
+            bra_max = std::max(bra_max, ket_table_bra_bytes(u->b->t.n));
             nobs_max = std::max(nobs_max, u->nobs);
         }
         for (const PairDesc& d : descs)  // imaginary parts are accumulated with one observable group only
             if (d.complex_out && nobs_max > 32)
                 raise(NSG_ERR_INVALID_ARGUMENT, nobs_max, 32, "complex pair sums take at most 32 observables per launch");
         // Tasks: about four per resident warp, never spanning two units.
-        const size_t warp_smem = pair_warp_smem_bytes(tab_max, wb);
+        const size_t warp_smem = pair_warp_smem_bytes(tab_max, bra_max, wb);
         const int64_t resident = pair_resident_warps(wb, nobs_max, warp_smem);
         int64_t total_chunks = 0;
         for (const PairDesc& d : descs) total_chunks += d.nchunks;
@@ -728,6 +732,7 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
         m.blocks = (int)std::max<int64_t>(1, (warps + wpb - 1) / wpb);
         m.nwarps = m.blocks * wpb;
         m.tab_bytes_max = tab_max;
+        m.bra_bytes_max = bra_max;
         m.warp_smem = warp_smem;
         if (sel.size() == 1) {
             m.dbg_k = dbg_k;

@@ -143,8 +143,10 @@ struct PairDesc {
     TermsView A;
     TermsView B;
     FrameView fr;                  // frames of A
-    const void* ktab = nullptr;    // ket tables of B
-    size_t ktab_stride = 0;
+    const void* ktab = nullptr;    // term tables of B (ket side)
+    const void* atab = nullptr;    // term tables of A (its G table is the bra side)
+    size_t ktab_stride = 0;        // bytes per term of both (A and B have the same width)
+    uint32_t ket_bytes = 0;        // the part of a term's tables the kernel copies per ket
     int ngrp = 0;
     int nobs = 0;
     const uint64_t* px = nullptr;  // [chiA][nobs] x_{A,P}
@@ -177,7 +179,8 @@ struct MultiLaunch {
     unsigned long long* counter = nullptr;  // zero before the launch
     int nwarps = 0;
     int blocks = 0;
-    size_t tab_bytes_max = 0;             // largest ket_table_stride among the units
+    size_t tab_bytes_max = 0;             // largest ket_bytes among the units
+    size_t bra_bytes_max = 0;             // largest bra (G) table among the units
     size_t warp_smem = 0;
     uint8_t* dbg_k = nullptr;             // single-unit per-pair dump [chiA][chiB]
     int32_t* dbg_r = nullptr;
@@ -190,7 +193,7 @@ cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_
 // out: 2 doubles (re, im) per observable, observables of unit u starting at obs_begin[u].
 cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, int64_t total_obs, double* out,
                                 cudaStream_t st);
-size_t pair_warp_smem_bytes(size_t tab_bytes_max, int word_bytes);
+size_t pair_warp_smem_bytes(size_t ket_bytes_max, size_t bra_bytes_max, int word_bytes);
 // Warps of the pair kernel resident on the whole device at once.
 int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem);
 
@@ -198,10 +201,12 @@ int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem);
 // per-term table storage; at most 32 observables).
 cudaError_t launch_pairs_rows(const PairLaunch& p, cudaStream_t st);
 
-// Ket tables: per term, Four-Russians tables of G, F, M and the ordered-sign
-// matrix P (n ≤ 64); sizes below.
+// Term tables: per term, Four-Russians tables of F, the ordered-sign matrix
+// P, K = M·Fᵀ and G, plus the term's scalars (n ≤ 64); sizes below.
 int ket_table_groups(int n);
-size_t ket_table_stride(int n);
+size_t ket_table_stride(int n);      // bytes per term
+size_t ket_table_ket_bytes(int n);   // the leading part read per ket (F, P, K tables and scalars)
+size_t ket_table_bra_bytes(int n);   // the trailing G table, read per bra
 cudaError_t launch_ket_tables(const TermsView& t, void* out, cudaStream_t st);
 
 // Reduce per-warp partials to one value (re, im) per observable, scaled by

@@ -254,12 +254,15 @@ struct ChunkAcc {
 };
 
 // ---- ket tables -----------------------------------------------------------------
-// Per term B: Four-Russians tables of its rows, 16 XOR combinations of each
-// group of four rows, for the matrices G, F, M and P, where P[q] holds the
-// bits r > q with parity(M_q·F_r) (so that Σ_{q<r∈f} M_q·F_r =
-// parity((f·P) ∧ f)).  Layout per term: [4][ngrp][16] Words, then a
-// 48-byte trailer with the term's scalars (KetTrailer), so one bulk copy
-// brings everything the pair kernel reads of a ket.
+// Per term B, Four-Russians tables (the 16 XOR combinations of each group of
+// four rows) of three matrices the pair kernel multiplies by:
+//   F        the tableau's F rows,
+//   P        P[c] = the bits r > c of K[c]  (ordered-sign matrix),
+//   K        K[c][r] = parity(M_c·F_r), i.e. K = M·F^T,
+// then a 48-byte trailer with the term's scalars (KetTrailer), and last the
+// table of G, which the pair kernel reads when the term is the bra.  Layout
+// per term: [F|P|K][ngrp][16] Words, trailer, [G][ngrp][16] Words; one bulk
+// copy of the first part brings everything the kernel reads of a ket.
 struct KetTrailer {
     uint64_t gl, gh, v, s;  // γ planes, v, s (low word)
     uint8_t phase, coef_k, pad0, pad1;
@@ -271,30 +274,45 @@ static_assert(sizeof(KetTrailer) == 48, "trailer size");
 template <typename Word>
 __global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, int ngrp, size_t stride,
                                                                  unsigned char* __restrict__ out) {
-    __shared__ Word sR[FWARPS][4][64];
+    __shared__ Word sR[FWARPS][4][64];  // F, P, K, G
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t term = (int64_t)blockIdx.x * FWARPS + wid;
     if (term >= tv.chi) return;
     const int n = tv.n;
     for (int r = lane; r < 64; r += 32) {
         size_t idx = ((size_t)term * tv.R + r) * tv.W;
-        sR[wid][0][r] = (Word)tv.G[idx];
-        sR[wid][1][r] = (Word)tv.F[idx];
-        sR[wid][2][r] = (Word)tv.M[idx];
+        sR[wid][0][r] = (Word)tv.F[idx];
+        sR[wid][2][r] = (Word)tv.M[idx];  // M, replaced by K below
+        sR[wid][3][r] = (Word)tv.G[idx];
     }
     __syncwarp();
-    for (int q = lane; q < 64; q += 32) {
-        Word pq = 0;
-        if (q < n) {
-            const Word mq = sR[wid][2][q];
-            for (int r = q + 1; r < n; r++) pq |= (Word)(popc<Word>(mq & sR[wid][1][r]) & 1) << r;
+    Word kr[2];
+    for (int t = 0; t < 2; t++) {
+        const int c = lane + 32 * t;
+        Word k = 0;
+        if (c < n) {
+            const Word mc = sR[wid][2][c];
+            for (int r = 0; r < n; r++) k |= (Word)(popc<Word>(mc & sR[wid][0][r]) & 1) << r;
         }
-        sR[wid][3][q] = pq;
+        kr[t] = k;
     }
     __syncwarp();
-    const int per = ngrp * 16, total = 4 * per;
-    Word* dst = (Word*)(out + (size_t)term * stride);
-    for (int e = lane; e < total; e += 32) {
+    for (int t = 0; t < 2; t++) {
+        const int c = lane + 32 * t;
+        if (c < 8 * (int)sizeof(Word)) {
+            sR[wid][2][c] = kr[t];
+            sR[wid][1][c] = (c + 1 < 8 * (int)sizeof(Word)) ? (kr[t] & ~(((Word)1 << (c + 1)) - 1)) : (Word)0;
+        } else {
+            sR[wid][2][c] = 0;
+            sR[wid][1][c] = 0;
+        }
+    }
+    __syncwarp();
+    const int per = ngrp * 16;
+    unsigned char* base = out + (size_t)term * stride;
+    Word* dst = (Word*)base;
+    Word* gdst = (Word*)(base + 3 * per * sizeof(Word) + sizeof(KetTrailer));
+    for (int e = lane; e < 4 * per; e += 32) {
         const int mat = e / per, g = (e / 16) % ngrp, idx = e & 15;
         Word acc = 0;
 #pragma unroll
@@ -302,7 +320,8 @@ __global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, i
             const int row = 4 * g + b;
             if (((idx >> b) & 1) && row < n) acc ^= sR[wid][mat][row];
         }
-        dst[e] = acc;
+        if (mat < 3) dst[e] = acc;
+        else gdst[e - 3 * per] = acc;
     }
     if (lane == 0) {
         KetTrailer t;
@@ -315,14 +334,14 @@ __global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, i
         t.pad0 = t.pad1 = 0;
         t.coef_r = tv.coef_r[term];
         t.pad2 = 0;
-        *(KetTrailer*)(dst + total) = t;
+        *(KetTrailer*)(dst + 3 * per) = t;
     }
 }
 
 // ---- pair kernel ---------------------------------------------------------------
-// Shared memory per warp: two table buffers (double-buffered TMA bulk copies
-// of the next ket's tables), the transformed ket's F and M rows, and one
-// mbarrier per buffer.
+// Shared memory per warp: two ket buffers (double-buffered bulk copies of the
+// next ket's tables), the bra's G table, the composed F and J rows (for the
+// per-observable start values), and one mbarrier per ket buffer.
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar) {
@@ -356,111 +375,93 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
 }
 
 template <typename Word>
-__device__ __forceinline__ Word lsb(Word x) {  // lowest set bit as a mask
-    return x & ((Word)0 - x);
-}
-
-template <typename Word>
 __device__ __forceinline__ int parity(Word x) {
     return popc<Word>(x) & 1;
-}
-
-// left_multiply_h (h.rs:13-65) + _resolve_superposition (resolve_superposition.rs:6-176)
-// on a warp-held tableau with one word per row.  The commuting column
-// operations of the basis transform are applied as one masked update; the
-// pivot is the lowest set bit of D0 (else D1), as in the reference.
-template <typename Word, int RPL>
-__device__ __forceinline__ void pair_h(Word (&G)[RPL], Word (&F)[RPL], Word (&M)[RPL], uint32_t& gam, Word& v,
-                                       Word& s, int& phase, int q, int& err) {
-    const int sl = q >> 5, src = q & 31;
-    Word g0 = G[0], f0 = F[0], m0 = M[0];
-    uint32_t gg = gam;
-    if (RPL > 1 && sl) {
-        g0 = G[RPL - 1];
-        f0 = F[RPL - 1];
-        m0 = M[RPL - 1];
-        gg = gam >> 2;
-    }
-    const Word Gq = shfl<Word>(g0, src), Fq = shfl<Word>(f0, src), Mq = shfl<Word>(m0, src);
-    const int gq = (int)(shfl<uint32_t>(gg, src) & 3);
-    const Word nv = ~v;
-    const Word t = s ^ (Gq & v);
-    const Word u = s ^ (Fq & nv) ^ (Mq & v);
-    const int alpha = parity<Word>(Gq & nv & s);
-    const int beta = parity<Word>((Mq & nv & s) ^ (Fq & v & (Mq ^ s)));
-    const int delta = (2 * gq + 4 * (alpha ^ beta)) & 7;
-    phase = (phase + 4 * alpha) & 7;
-    const Word d = t ^ u;
-    if (d == 0) {  // handle_same_vecs_case :115-133
-        if (delta == 4) err = 1;
-        s = t;
-        phase = (phase + (delta == 2 ? 1 : (delta == 6 ? 7 : 0))) & 7;
-        return;
-    }
-    const Word d0 = d & nv, d1 = d & v;
-    Word pm;
-    if (d0) {
-        pm = lsb<Word>(d0);
-        const Word rest = d0 ^ pm;
-#pragma unroll
-        for (int k = 0; k < RPL; k++) {
-            const bool fb = (F[k] & pm) != 0;
-            const int par1 = parity<Word>(F[k] & d1);
-            if (parity<Word>(G[k] & rest)) G[k] ^= pm;
-            if (parity<Word>(M[k] & rest) ^ par1) M[k] ^= pm;
-            if (fb) {
-                F[k] ^= rest;
-                M[k] ^= d1;
-                if (par1) gam ^= 2u << (2 * k);
-            }
-        }
-    } else {
-        pm = lsb<Word>(d1);
-        const Word rest = d1 ^ pm;
-#pragma unroll
-        for (int k = 0; k < RPL; k++) {
-            if (G[k] & pm) G[k] ^= rest;
-            if (parity<Word>(F[k] & rest)) F[k] ^= pm;
-            if (M[k] & pm) M[k] ^= rest;
-        }
-    }
-    const bool vp = (v & pm) != 0;
-    s = (t & pm) ? u : t;
-    bool sp, vnew = vp, rs = false;
-    int dph = 0;
-    if (t & pm) {
-        switch (delta) {
-            case 0: sp = false; vnew = !vp; break;
-            case 4: sp = true; vnew = !vp; dph = 4; break;
-            case 2: if (vp) { dph = 1; sp = false; } else { sp = true; vnew = true; dph = 2; } rs = true; break;
-            default: if (vp) { dph = 7; sp = true; } else { sp = false; vnew = true; dph = 6; } rs = true; break;
-        }
-    } else {
-        switch (delta) {
-            case 0: sp = false; vnew = !vp; break;
-            case 4: sp = true; vnew = !vp; break;
-            case 2: if (vp) { dph = 1; sp = true; } else { sp = false; vnew = true; } rs = true; break;
-            default: if (vp) { dph = 7; sp = false; } else { sp = true; vnew = true; } rs = true; break;
-        }
-    }
-    s = sp ? (s | pm) : (s & ~pm);
-    v = vnew ? (v | pm) : (v & ~pm);
-    phase = (phase + dph) & 7;
-    if (rs) {  // right_multiply_s(pivot) (right_multiplication/s.rs:8-24)
-#pragma unroll
-        for (int k = 0; k < RPL; k++) {
-            if (F[k] & pm) {
-                M[k] ^= pm;
-                const uint32_t gk = (gam >> (2 * k)) & 3;
-                gam = (gam & ~(3u << (2 * k))) | (((gk + 3) & 3) << (2 * k));
-            }
-        }
-    }
 }
 
 template <typename Word, int RPL>
 __device__ __forceinline__ int nib(const Word x, int g) {  // 4-bit group g of a row
     return (int)((x >> (4 * g)) & 15);
+}
+
+// 32×32 bit-matrix transpose across a warp (lane l holds row l; returns row
+// l of the transpose): five rounds of block swaps between lanes l and l^j.
+__device__ __forceinline__ uint32_t transpose32(uint32_t x, int lane) {
+    const uint32_t m[5] = {0x0000ffffu, 0x00ff00ffu, 0x0f0f0f0fu, 0x33333333u, 0x55555555u};
+#pragma unroll
+    for (int t = 0; t < 5; t++) {
+        const int j = 16 >> t;
+        const uint32_t y = __shfl_xor_sync(FULL, x, j);
+        x = (lane & j) ? ((x & ~m[t]) | ((y >> j) & m[t])) : ((x & m[t]) | ((y << j) & ~m[t]));
+    }
+    return x;
+}
+
+// Transpose of a strictly lower-triangular matrix held as rows (lane, slot):
+// one word per row for n ≤ 32, rows l and l+32 for n ≤ 64 (the upper-right
+// 32×32 block is zero).
+__device__ __forceinline__ void transpose_lower(const uint32_t (&L)[1], uint32_t (&T)[1], int lane) {
+    T[0] = transpose32(L[0], lane);
+}
+__device__ __forceinline__ void transpose_lower(const uint64_t (&L)[2], uint64_t (&T)[2], int lane) {
+    const uint32_t a = transpose32((uint32_t)L[0], lane);          // rows 0-31, cols 0-31
+    const uint32_t c = transpose32((uint32_t)L[1], lane);          // rows 32-63, cols 0-31
+    const uint32_t dd = transpose32((uint32_t)(L[1] >> 32), lane); // rows 32-63, cols 32-63
+    T[0] = (uint64_t)a | ((uint64_t)c << 32);
+    T[1] = (uint64_t)dd << 32;
+}
+
+template <typename Word, int RPL>
+__device__ __forceinline__ Word row_of(const Word (&R)[RPL], int q) {  // row q, from its lane
+    return shfl<Word>((RPL > 1 && q >= 32) ? R[RPL - 1] : R[0], q & 31);
+}
+
+// The exponential sum Σ_z i^{L·z}·(-1)^{Σ_{a<b} J_ab z_a z_b} over the alive
+// variables is reduced one variable at a time.  L = L0 + 2·h (mod 4): the low
+// bits L0, the matrix J and the pivots are shared by all observables; the high
+// bits split into a shared part hs and a per-observable part h[g].
+//
+// expand(T): multiply by i^{±τ}, τ = ⊕_{a∈T} z_a, using
+// τ = Σ_a z_a − 2·Σ_{a<b} z_a z_b (mod 4): J ^= T·Tᵀ off the diagonal and
+// L_a ± 1 on T (the per-observable part of the carry is applied by the caller).
+template <typename Word, int RPL>
+__device__ __forceinline__ void g_expand(Word (&J)[RPL], Word& hs, Word& L0, Word T, const Word (&own)[RPL]) {
+#pragma unroll
+    for (int k = 0; k < RPL; k++)
+        if (T & own[k]) J[k] ^= T & ~own[k];
+    hs ^= T & ~L0;
+    L0 ^= T;
+}
+
+// subst: eliminate z_k = c ⊕ lp·z (c per observable) from the form.
+template <typename Word, int RPL, int NG>
+__device__ __forceinline__ void g_subst(int kq, Word lp, const bool (&c)[NG], Word (&J)[RPL], Word& hs, Word& L0,
+                                        Word& alive, Word (&h)[NG], int (&ph)[NG], const Word (&own)[RPL]) {
+    const Word kb = (Word)1 << kq;
+    const Word R = row_of<Word, RPL>(J, kq) & alive & ~kb;
+#pragma unroll
+    for (int k = 0; k < RPL; k++) {  // z_k·(R·z) → (lp·z)(R·z): J ^= lp·Rᵀ + R·lpᵀ
+        Word u = 0;
+        if (lp & own[k]) u ^= R;
+        if (R & own[k]) u ^= lp;
+        J[k] ^= u;
+    }
+    hs ^= lp & R;  // its diagonal terms z_a² = z_a
+    const bool lowk = (L0 >> kq) & 1, hsk = (hs >> kq) & 1;
+    alive &= ~kb;
+#pragma unroll
+    for (int g = 0; g < NG; g++) {
+        if (c[g]) h[g] ^= R;
+        const bool hb = hsk ^ (bool)((h[g] >> kq) & 1);
+        if (!lowk) {  // (-1)^{hb·(c ⊕ lp·z)}
+            if (hb && c[g]) ph[g] += 4;
+            if (hb) h[g] ^= lp;
+        } else {  // i^{L_k·(c ⊕ lp·z)} = i^{L_k c}·i^{±lp·z}
+            if (c[g]) ph[g] += hb ? 6 : 2;
+            if (hb == c[g]) h[g] ^= lp;
+        }
+    }
+    if (lowk) g_expand<Word, RPL>(J, hs, L0, lp, own);
 }
 
 template <typename Word, int RPL, int NG>
@@ -472,9 +473,10 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
     unsigned char* wbase = smem_raw + (size_t)wid * p.warp_smem;
     Word* tb0 = (Word*)wbase;
     Word* tb1 = (Word*)(wbase + p.tab_bytes_max);
-    Word* sF = (Word*)(wbase + 2 * p.tab_bytes_max);
-    Word* sM = sF + 64;
-    uint64_t* bars = (uint64_t*)(sM + 64);
+    Word* tbA = (Word*)(wbase + 2 * p.tab_bytes_max);  // the bra's G table
+    Word* sF = (Word*)(wbase + 2 * p.tab_bytes_max + p.bra_bytes_max);
+    Word* sJ = sF + 64;
+    uint64_t* bars = (uint64_t*)(sJ + 64);
     if (lane == 0) {
         mbar_init(&bars[0]);
         mbar_init(&bars[1]);
@@ -482,6 +484,10 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
     }
     __syncwarp();
     uint32_t par0 = 0, par1 = 0;  // next phase parity per buffer
+
+    Word own[RPL];  // this lane's row bits
+#pragma unroll
+    for (int k = 0; k < RPL; k++) own[k] = (Word)1 << (32 * k + lane);
 
     // current descriptor
     int ds = -1;
@@ -493,9 +499,9 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
     bool tri = true, cplx = false;
 
     int64_t cur_i = -1;
-    Word GV[RPL], FV[RPL], MV[RPL];
+    Word FV[RPL], MV[RPL];
     uint32_t gamV = 0;
-    Word vA = 0, sA = 0;
+    Word vA = 0;
     int kcA = 0, rcA = 0;
     Word xs[NG];
     int ks[NG];
@@ -518,7 +524,7 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
             ds = lo;
             d = p.descs + ds;
             ktab = (const unsigned char*)d->ktab;
-            tab_bytes = (uint32_t)d->ktab_stride;
+            tab_bytes = d->ket_bytes;
             n = d->A.n;
             ngrp = d->ngrp;
             nobs = d->nobs;
@@ -546,13 +552,12 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
                 j0 = (lc % d->cpr) * p.chunk;
             }
             j1 = min(j0 + (int64_t)p.chunk, chiB);
-            if (i != cur_i) {
+            if (i != cur_i) {  // a new bra: its frame rows, scalars, Pauli frames and G table
                 cur_i = i;
                 const FrameView& fr = d->fr;
 #pragma unroll
                 for (int k = 0; k < RPL; k++) {
                     size_t o = (size_t)i * 64 + 32 * k + lane;
-                    GV[k] = (Word)fr.GV[o];
                     FV[k] = (Word)fr.FV[o];
                     MV[k] = (Word)fr.MV[o];
                 }
@@ -565,7 +570,6 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
                 }
                 const TermsView& A = d->A;
                 vA = (Word)A.V[i * A.W];
-                sA = (Word)A.S[i * A.W];
                 kcA = A.coef_k[i];
                 rcA = A.coef_r[i];
 #pragma unroll
@@ -574,6 +578,9 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
                     xs[g] = (o < nobs) ? (Word)d->px[(size_t)i * nobs + o] : (Word)0;
                     ks[g] = (o < nobs) ? d->pk[(size_t)i * nobs + o] : 0;
                 }
+                const Word* ga = (const Word*)((const unsigned char*)d->atab + (size_t)i * d->ktab_stride + tab_bytes);
+                for (int e = lane; e < ngrp * 16; e += 32) tbA[e] = ga[e];
+                __syncwarp();
             }
             constexpr int NA = (NG == 1) ? 4 : 2;
             ChunkAcc<NG, NA> acc;
@@ -582,13 +589,14 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
             // first ket of the chunk
             if (lane == 0) {
                 fence_proxy_async();
-                tma_load(buf ? tb1 : tb0, ktab + (size_t)j0 * tab_bytes, tab_bytes, buf ? &bars[1] : &bars[0]);
+                tma_load(buf ? tb1 : tb0, ktab + (size_t)j0 * d->ktab_stride, tab_bytes, buf ? &bars[1] : &bars[0]);
             }
             for (int64_t j = j0; j < j1; j++) {
                 // prefetch the next ket's tables into the other buffer
                 if (j + 1 < j1 && lane == 0) {
                     fence_proxy_async();
-                    tma_load(buf ? tb0 : tb1, ktab + (size_t)(j + 1) * tab_bytes, tab_bytes, buf ? &bars[0] : &bars[1]);
+                    tma_load(buf ? tb0 : tb1, ktab + (size_t)(j + 1) * d->ktab_stride, tab_bytes,
+                             buf ? &bars[0] : &bars[1]);
                 }
                 bool ok_wait;
                 if (buf) {
@@ -610,113 +618,168 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
                     break;
                 }
                 const Word* T = buf ? tb1 : tb0;
-                const KetTrailer& kt = *(const KetTrailer*)(T + 4 * ngrp * 16);  // the ket's scalars
-                const Word glB = (Word)kt.gl, ghB = (Word)kt.gh;
-                Word v = (Word)kt.v, s = (Word)kt.s;
-                int phase = kt.phase;
-                const int kcB = kt.coef_k, rcB = kt.coef_r;
+                const KetTrailer& kt = *(const KetTrailer*)(T + 3 * ngrp * 16);  // the ket's scalars
+                const Word glB = (Word)kt.gl, ghB = (Word)kt.gh, vB = (Word)kt.v, sB = (Word)kt.s;
+                const int phB = kt.phase, kcB = kt.coef_k, rcB = kt.coef_r;
 
-                // ---- D = V·U_B by table lookups (Four Russians)
-                Word gD[RPL], fD[RPL], mD[RPL], y[RPL];
+                // ---- D = V·U_B (Four Russians): F_D = F_V·F_B, y = F_V·P_B,
+                //      K = M_D·F_Dᵀ = (F_V·K_B ⊕ M_V)·G_A  (G_B·F_Bᵀ = I, F_Vᵀ = G_A)
+                Word fD[RPL], yP[RPL], Y[RPL], Kr[RPL];
 #pragma unroll
-                for (int k = 0; k < RPL; k++) gD[k] = fD[k] = mD[k] = y[k] = 0;
+                for (int k = 0; k < RPL; k++) {
+                    fD[k] = yP[k] = Kr[k] = 0;
+                    Y[k] = MV[k];
+                }
 #pragma unroll
                 for (int g = 0; g < GMAX; g++) {
                     if (g < ngrp) {
-                        const Word* TG = T + g * 16;
-                        const Word* TF = T + (ngrp + g) * 16;
-                        const Word* TM = T + (2 * ngrp + g) * 16;
-                        const Word* TP = T + (3 * ngrp + g) * 16;
+                        const Word* TF = T + g * 16;
+                        const Word* TP = T + (ngrp + g) * 16;
+                        const Word* TK = T + (2 * ngrp + g) * 16;
 #pragma unroll
                         for (int k = 0; k < RPL; k++) {
-                            const int ig = nib<Word, RPL>(GV[k], g), jf = nib<Word, RPL>(FV[k], g),
-                                      im = nib<Word, RPL>(MV[k], g);
-                            gD[k] ^= TG[ig];
+                            const int jf = nib<Word, RPL>(FV[k], g);
                             fD[k] ^= TF[jf];
-                            mD[k] ^= TM[jf] ^ TG[im];
-                            y[k] ^= TP[jf];
+                            yP[k] ^= TP[jf];
+                            Y[k] ^= TK[jf];
                         }
                     }
                 }
-                uint32_t gam = 0;
+#pragma unroll
+                for (int g = 0; g < GMAX; g++) {
+                    if (g < ngrp) {
+#pragma unroll
+                        for (int k = 0; k < RPL; k++) Kr[k] ^= tbA[g * 16 + nib<Word, RPL>(Y[k], g)];
+                    }
+                }
+                // γ_D (eq. of the composed tableau) and the uniform bit planes
+                Word g0 = 0, g1 = 0, diag = 0, fvs = 0, Lw[RPL];
+                const Word w = vB & sB;
 #pragma unroll
                 for (int k = 0; k < RPL; k++) {
                     const int gsum = popc<Word>(FV[k] & glB) + 2 * popc<Word>(FV[k] & ghB);
-                    const int g = (int)((gamV >> (2 * k)) & 3) + gsum + 2 * parity<Word>(y[k] & FV[k]);
-                    gam |= (uint32_t)(g & 3) << (2 * k);
+                    const int gm = (int)((gamV >> (2 * k)) & 3) + gsum + 2 * parity<Word>(yP[k] & FV[k]);
+                    g0 |= (Word)__ballot_sync(FULL, gm & 1) << (32 * k);
+                    g1 |= (Word)__ballot_sync(FULL, gm & 2) << (32 * k);
+                    diag |= (Word)__ballot_sync(FULL, (Kr[k] & own[k]) != 0) << (32 * k);
+                    fvs |= (Word)__ballot_sync(FULL, parity<Word>(fD[k] & w)) << (32 * k);
+                    Lw[k] = Kr[k] & (own[k] - 1);
                 }
-
-                // ---- U_{H,A}
-                int err = 0;
-                Word hv = vA;
-                int errq = -1;
-                while (hv) {
-                    const int q = ffs0<Word>(hv);
-                    hv &= hv - 1;
-                    pair_h<Word, RPL>(gD, fD, mD, gam, v, s, phase, q, err);
-                    if (err && errq < 0) errq = q;
-                }
-                if (err && lane == 0) {
-                    atomicOr(d->status, DS_INVARIANT);
-                    if (atomicCAS(d->status + 1, 0, 1) == 0) {  // first hit: record where
-                        d->status[2] = (int)i;
-                        d->status[3] = (int)j;
-                        d->status[4] = errq;
-                    }
-                }
-
-                // ---- stage F, M rows of the transformed ket; γ planes by ballot
+                // J: the symmetric coupling matrix, J[a][b] = K[max][min]
+                Word J[RPL], LwT[RPL];
+                transpose_lower(Lw, LwT, lane);
 #pragma unroll
                 for (int k = 0; k < RPL; k++) {
+                    J[k] = Lw[k] | LwT[k];
                     sF[32 * k + lane] = fD[k];
-                    sM[32 * k + lane] = mD[k];
-                }
-                Word gl2 = 0, gh2 = 0;
-#pragma unroll
-                for (int k = 0; k < RPL; k++) {
-                    const uint32_t b0 = __ballot_sync(FULL, gam & (1u << (2 * k)));
-                    const uint32_t b1 = __ballot_sync(FULL, gam & (2u << (2 * k)));
-                    gl2 |= (Word)b0 << (32 * k);
-                    gh2 |= (Word)b1 << (32 * k);
+                    sJ[32 * k + lane] = J[k];
                 }
                 __syncwarp();
-                const int rv = popc<Word>(v);
 
-                // ---- amplitudes ⟨x|ket⟩: u = xF, m = xM, ordered sign Σ_{p<r∈x} M_p·F_r
-                //      (parity accumulated as an XOR of the masked products).
-                Word u[NG], mac[NG], sacc[NG];
+                const Word full = (n >= 8 * (int)sizeof(Word)) ? ~(Word)0 : (((Word)1 << n) - 1);
+                const Word cons = ~vB & full;
+                // ---- per-observable start: the fixed coordinates x' = x ∧ ¬v_A
+                Word h[NG], rhs[NG];
+                int ph[NG];
+                bool zero[NG];
 #pragma unroll
-                for (int g = 0; g < NG; g++) u[g] = mac[g] = sacc[g] = 0;
-                for (int q = 0; q < n; q++) {
-                    const Word f = sF[q], m = sM[q];
-                    const Word bit = (Word)1 << q;
+                for (int g = 0; g < NG; g++) {
+                    const Word x = xs[g], xf = x & ~vA & full;
+                    const int gx = popc<Word>(xf & g0) + 2 * popc<Word>(xf & g1);
+                    int qx = 0;
+                    Word xF = 0, Jx = 0, t = xf;
+                    while (t) {
+                        const int q = ffs0<Word>(t);
+                        t &= t - 1;
+                        const Word Jq = sJ[q];
+                        qx ^= parity<Word>(Jq & xf & (((Word)1 << q) - 1)) ^ (int)((diag >> q) & 1);
+                        xF ^= sF[q];
+                        Jx ^= Jq;
+                    }
+                    ph[g] = phB + 2 * gx + 4 * (qx ^ parity<Word>(xF & w));
+                    h[g] = (x ^ Jx) & vA;
+                    rhs[g] = (sB ^ xF) & cons;
+                    zero[g] = false;
+                }
+                __syncwarp();  // sF/sJ are rewritten by the next ket
+
+                // ---- the exponential sum over z ∈ span(v_A)
+                Word hs = (g1 ^ diag ^ fvs) & vA, L0 = g0 & vA, alive = vA;
+                int r = popc<Word>(vA) + popc<Word>(vB);
+                Word Fc[RPL];
 #pragma unroll
-                    for (int g = 0; g < NG; g++) {
-                        const Word sel = (xs[g] & bit) ? ~(Word)0 : (Word)0;
-                        const Word fs = f & sel;
-                        sacc[g] ^= mac[g] & fs;
-                        mac[g] ^= m & sel;
-                        u[g] ^= fs;
+                for (int k = 0; k < RPL; k++) Fc[k] = fD[k] & cons;
+                // constraints (z·F)_b = rhs_b for b ∉ v_B, by substitution
+                Word crem = cons;
+                while (crem) {
+                    const int b = ffs0<Word>(crem);
+                    crem &= crem - 1;
+                    Word l = 0;
+#pragma unroll
+                    for (int k = 0; k < RPL; k++) l |= (Word)__ballot_sync(FULL, (Fc[k] >> b) & 1) << (32 * k);
+                    l &= alive;
+                    bool c[NG];
+#pragma unroll
+                    for (int g = 0; g < NG; g++) c[g] = (rhs[g] >> b) & 1;
+                    if (l == 0) {  // a consistency condition
+#pragma unroll
+                        for (int g = 0; g < NG; g++) zero[g] |= c[g];
+                        continue;
+                    }
+                    const int kq = ffs0<Word>(l);
+                    const Word lp = l & (l - 1);
+                    const Word Fk = row_of<Word, RPL>(Fc, kq);
+#pragma unroll
+                    for (int k = 0; k < RPL; k++)
+                        if (lp & own[k]) Fc[k] ^= Fk;
+#pragma unroll
+                    for (int g = 0; g < NG; g++)
+                        if (c[g]) rhs[g] ^= Fk;
+                    g_subst<Word, RPL, NG>(kq, lp, c, J, hs, L0, alive, h, ph, own);
+                }
+                // summation, lowest alive variable first
+                while (alive) {
+                    const int jq = ffs0<Word>(alive);
+                    const Word jb = (Word)1 << jq;
+                    const Word S = row_of<Word, RPL>(J, jq) & alive & ~jb;
+                    const bool hsj = (hs >> jq) & 1;
+                    alive &= ~jb;
+                    bool hb[NG];
+#pragma unroll
+                    for (int g = 0; g < NG; g++) hb[g] = hsj ^ (bool)((h[g] >> jq) & 1);
+                    if ((L0 >> jq) & 1) {  // 1 + i^{L_j}(-1)^{S·z} = √2·ω^{±1}·i^{∓S·z}
+                        r -= 1;
+#pragma unroll
+                        for (int g = 0; g < NG; g++) {
+                            ph[g] += hb[g] ? 7 : 1;
+                            if (hb[g]) h[g] ^= S;
+                        }
+                        g_expand<Word, RPL>(J, hs, L0, S, own);
+                    } else {  // 1 + (-1)^{hb + S·z} = 2·δ(S·z = hb)
+                        r -= 2;
+                        if (S == 0) {
+#pragma unroll
+                            for (int g = 0; g < NG; g++) zero[g] |= hb[g];
+                        } else {
+                            g_subst<Word, RPL, NG>(ffs0<Word>(S), S & (S - 1), hb, J, hs, L0, alive, h, ph, own);
+                        }
                     }
                 }
+
                 const int kpair = (kcB - kcA) & 7;
-                const int rpair = rcA + rcB + rv;
+                const int rpair = rcA + rcB + r;
                 const int wgt = (tri && j != i) ? 2 : 1;
 #pragma unroll
                 for (int g = 0; g < NG; g++) {
                     const int o = 32 * g + lane;
-                    const bool ok = (((u[g] ^ s) & ~v) == 0);
-                    const int gsum = popc<Word>(xs[g] & gl2) + 2 * popc<Word>(xs[g] & gh2);
-                    const int sg = parity<Word>(sacc[g] ^ (u[g] & mac[g]) ^ (u[g] & v & s));
-                    const int kamp = (phase + 2 * gsum + 4 * sg) & 7;
                     if (p.dbg_k && o == 0) {
                         const size_t di = (size_t)i * chiB + j;
-                        p.dbg_k[di] = ok ? (uint8_t)((ks[g] + kamp) & 7) : (uint8_t)255;
-                        p.dbg_r[di] = rv;
+                        p.dbg_k[di] = zero[g] ? (uint8_t)255 : (uint8_t)((ks[g] + ph[g]) & 7);
+                        p.dbg_r[di] = r;
                     }
-                    if (ok && o < nobs) {
+                    if (!zero[g] && o < nobs) {
                         double* pp = rec + (size_t)o * 8;
-                        const int k = (kpair + ks[g] + kamp) & 7;
+                        const int k = (kpair + ks[g] + ph[g]) & 7;
                         int sgn, m;
                         re_part(k, rpair, sgn, m);
                         if (sgn) acc.add(g, m & 1, sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1), p.mixed, pp);
@@ -728,7 +791,7 @@ __global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
                         }
                     }
                 }
-                __syncwarp();  // all lanes done with buffer `buf` and the staged rows
+                __syncwarp();  // all lanes done with buffer `buf`
                 buf ^= 1;
             }
             // ---- fold the chunk into the task's double-double record
@@ -1157,9 +1220,13 @@ cudaError_t launch_pauli_frames(const TermsView& t, const DevPauli* d_paulis, in
 
 static int pair_word_bytes(int n) { return n <= 32 ? 4 : 8; }
 
-size_t ket_table_stride(int n) {  // bytes per term: [4][ngrp][16] words + trailer
+size_t ket_table_stride(int n) {  // bytes per term: [F|P|K][ngrp][16] words, trailer, [G][ngrp][16] words
     return (size_t)4 * ket_table_groups(n) * 16 * pair_word_bytes(n) + sizeof(KetTrailer);
 }
+
+size_t ket_table_ket_bytes(int n) { return (size_t)3 * ket_table_groups(n) * 16 * pair_word_bytes(n) + sizeof(KetTrailer); }
+
+size_t ket_table_bra_bytes(int n) { return (size_t)ket_table_groups(n) * 16 * pair_word_bytes(n); }
 
 int ket_table_groups(int n) { return n <= 0 ? 1 : (n + 3) / 4; }
 
@@ -1202,8 +1269,8 @@ cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, 
     return cudaGetLastError();
 }
 
-size_t pair_warp_smem_bytes(size_t tab_bytes_max, int word_bytes) {
-    size_t b = 2 * tab_bytes_max + 2 * 64 * (size_t)word_bytes + 2 * sizeof(uint64_t);
+size_t pair_warp_smem_bytes(size_t ket_bytes_max, size_t bra_bytes_max, int word_bytes) {
+    size_t b = 2 * ket_bytes_max + bra_bytes_max + 2 * 64 * (size_t)word_bytes + 2 * sizeof(uint64_t);
     return (b + 127) & ~(size_t)127;
 }
 
