@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-METRIC = "Pauli <P>/s (64 observables, full chi^2 pair sum, n=40 t=24)"
+METRIC = "Pauli \u27e8P\u27e9/s and CH inner products/s, mixed+batched vs plain FP64 @\u22641e-9 err"
 UNIT = "<P>/s"
 
 
@@ -305,6 +305,227 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# The precision, batching and projection/sampling workloads (one JSON line each)
+def _setup_gpu():
+    import torch
+    from stab_decomp_simulator_rust_gb300 import _ffi, build
+    torch.cuda.set_device(0)
+    build.build()
+    return torch, _ffi.load()
+
+
+def _timed(torch, stream, fn, steps):
+    """Device time per call of fn() on `stream` (CUDA events), and its last result."""
+    out = None
+    tot = 0.0
+    for _ in range(steps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = fn()
+        e1.record(stream)
+        e1.synchronize()
+        tot += e0.elapsed_time(e1)
+    return tot / steps, out
+
+
+def _rel_err(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    return np.abs(a - b) / np.maximum(np.abs(b), 1e-300)
+
+
+def run_precision60(args, torch, L):
+    """n=60, 6000 {H,S,CX} + 36 T, 256 sparse Paulis of weight 1..8: FP64 and
+    mixed accumulation over the full χ² pair sum; per-observable error of the
+    mixed result against the FP64 one."""
+    from stab_decomp_simulator_rust_gb300 import PRECISION_FP64, PRECISION_MIXED, PauliString, QuantumState
+    from stab_decomp_simulator_rust_gb300 import workloads as W
+    cfg = W.PRECISION_N60
+    gates = W.random_clifford_t_circuit(cfg["n"], cfg["num_clifford"], cfg["num_t"], cfg["seed"])
+    sp = W.random_sparse_paulis(cfg["n"], cfg["num_paulis"], 1, 8, cfg["seed"] + 100)
+    paulis = [PauliString.sparse(o, q) for o, q in sp]
+    stream = torch.cuda.current_stream()
+    t0 = time.perf_counter()
+    st = QuantumState.from_gates(cfg["n"], gates)
+    compile_s = time.perf_counter() - t0
+    st.set_stream(stream.cuda_stream)
+    chi = st.stabilizer_rank
+    pairs = chi * (chi + 1) // 2
+    for _ in range(args.warmup):
+        st.exp_values(paulis[:32], PRECISION_MIXED)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms64, v64 = _timed(torch, stream, lambda: st.exp_values(paulis, PRECISION_FP64), args.steps)
+    msmx, vmx = _timed(torch, stream, lambda: st.exp_values(paulis, PRECISION_MIXED), args.steps)
+    ms1, _ = _timed(torch, stream, lambda: st.exp_value(paulis[0]), 1)
+    clocks.stop()
+    err = _rel_err(vmx, v64)
+    nobs = len(paulis)
+    line = {"metric": METRIC, "value": nobs / (msmx * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": msmx, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 accumulation of exact pair values, f64 final reduction",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": "n=60, 6000 {H,S,CX} + 36 T (seed 3), 256 sparse Paulis of weight 1..8 (seed 103)",
+                       "chi": chi, "pairs_per_observable": pairs, "compile_s": compile_s,
+                       "l2": "inputs larger than L2 (term tables)"},
+            "inner_products_per_s": nobs * pairs / (msmx * 1e-3),
+            "fp64": {"value": nobs / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64},
+            "plain": {"value": 1.0 / (ms1 * 1e-3), "unit": UNIT, "path": "nsg_exp_value, one observable per call"},
+            "mixed_rel_err_vs_fp64": {"max": float(err.max()), "median": float(np.median(err)),
+                                      "per_observable": [float(x) for x in err]},
+            "clocks": clocks.summary(), "gpu_launches": 3 * args.steps}
+    print(json.dumps(line))
+
+
+def run_batch512(args, torch, L):
+    """512 circuits, n ~ U[8, 64], t ~ U[4, 32], 20·n Clifford gates, 16 dense
+    Paulis each: every ⟨P⟩ of every circuit in one persistent launch per row
+    width (nsg_exp_value_multi), against the plain path run per circuit and
+    per observable (nsg_exp_value)."""
+    from stab_decomp_simulator_rust_gb300 import (PRECISION_FP64, PRECISION_MIXED, PauliString, QuantumState,
+                                                  exp_values_multi)
+    from stab_decomp_simulator_rust_gb300 import workloads as W
+    circuits = W.batch_circuits()
+    stream = torch.cuda.current_stream()
+    pinned = [torch.from_numpy(np.ascontiguousarray(g)).pin_memory().numpy() for _, g, _ in circuits]
+    t0 = time.perf_counter()
+    states = [QuantumState.from_gates(n, g) for (n, _, _), g in zip(circuits, pinned)]
+    compile_s = time.perf_counter() - t0
+    for s in states:
+        s.set_stream(stream.cuda_stream)
+    plists = [[PauliString.dense(p) for p in ps] for _, _, ps in circuits]
+    chis = [s.stabilizer_rank for s in states]
+    pairs = sum(c * (c + 1) // 2 for c in chis)
+    nobs = sum(len(p) for p in plists)
+    for _ in range(args.warmup):
+        exp_values_multi(states, plists, PRECISION_MIXED)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(0)
+    clocks.start()
+    msmx, vmx = _timed(torch, stream, lambda: exp_values_multi(states, plists, PRECISION_MIXED), args.steps)
+    ms64, v64 = _timed(torch, stream, lambda: exp_values_multi(states, plists, PRECISION_FP64), args.steps)
+    # plain: one circuit and one observable per call, FP64
+    npl = min(args.plain_circuits, len(states))
+
+    def plain():
+        return [[states[c].exp_value(p) for p in plists[c]] for c in range(npl)]
+    mspl, vpl = _timed(torch, stream, plain, 1)
+    clocks.stop()
+    obs_pl = sum(len(plists[c]) for c in range(npl))
+    err = np.concatenate([_rel_err(a, b) for a, b in zip(vmx, v64)])
+    err_pl = np.concatenate([_rel_err(np.asarray(vpl[c]), v64[c]) for c in range(npl)])
+    # end to end: compile from pinned host gate lists + the batched call
+    t0 = time.perf_counter()
+    st2 = [QuantumState.from_gates(n, g) for (n, _, _), g in zip(circuits, pinned)]
+    exp_values_multi(st2, plists, PRECISION_MIXED)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    del st2
+    line = {"metric": METRIC, "value": nobs / (msmx * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": msmx, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 accumulation of exact pair values, f64 final reduction",
+            "data": "synthetic (seeded generator)",
+            "config": {"workload": "512 circuits, n~U[8,64], t~U[4,32], 20n {H,S,CX}, 16 dense Paulis each (seed 4)",
+                       "chi_min": min(chis), "chi_max": max(chis), "chi_sum": sum(chis), "pairs_total": pairs,
+                       "observables": nobs, "l2": "inputs larger than L2 (term tables of 512 states)",
+                       "compile_s_all_circuits": compile_s},
+            "inner_products_per_s": sum(c * (c + 1) // 2 * len(p) for c, p in zip(chis, plists)) / (msmx * 1e-3),
+            "fp64_batched": {"value": nobs / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64},
+            "plain": {"value": obs_pl / (mspl * 1e-3), "unit": UNIT, "circuits": npl, "ms": mspl,
+                      "path": "nsg_exp_value per circuit and observable, FP64"},
+            "speedup_mixed_batched_vs_plain": (nobs / (msmx * 1e-3)) / (obs_pl / (mspl * 1e-3)),
+            "rel_err": {"mixed_vs_fp64_batched_max": float(err.max()), "plain_vs_fp64_batched_max": float(err_pl.max())},
+            "e2e": {"value": nobs / e2e_s, "unit": UNIT, "s": e2e_s,
+                    "h2d_bytes_per_step": int(sum(g.nbytes for g in pinned) + sum(p.ops.nbytes for ps in plists for p in ps)),
+                    "d2h_bytes_per_step": int(8 * nobs),
+                    "path": "nsg_state_from_circuit x512 + nsg_exp_value_multi, host buffers"},
+            "clocks": clocks.summary()}
+    print(json.dumps(line))
+
+
+def run_project64(args, torch, L):
+    """n=64, 8000 {H,S,CX} + 40 T: project qubits 0-7 onto seeded outcomes
+    (the last projection renormalises in FP64), then 10^6 samples of qubits
+    8-15.  The samples come from one pass over the 256 Z-strings on 8-15; the
+    same pass in mixed precision is compared with FP64, and the sample
+    histogram with the FP64 marginal (total-variation distance)."""
+    from stab_decomp_simulator_rust_gb300 import PRECISION_FP64, PRECISION_MIXED, PauliString, QuantumState
+    from stab_decomp_simulator_rust_gb300 import workloads as W
+    cfg = W.PROJECT_N64
+    n = cfg["n"]
+    gates = W.random_clifford_t_circuit(n, cfg["num_clifford"], cfg["num_t"], cfg["seed"])
+    rng = W.Xoshiro256ss(cfg["seed"] + 200)
+    outcomes = [rng.below(2) for _ in range(cfg["num_project"])]
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler(0)
+    clocks.start()
+    t0 = time.perf_counter()
+    st = QuantumState.from_gates(n, gates)
+    torch.cuda.synchronize()
+    compile_s = time.perf_counter() - t0
+    st.set_stream(stream.cuda_stream)
+    chi0 = st.stabilizer_rank
+
+    def project():
+        for q, o in enumerate(outcomes[:-1]):
+            st.project_unnormalized(q, bool(o))
+        st.project_normalized(len(outcomes) - 1, bool(outcomes[-1]))
+    ms_proj, _ = _timed(torch, stream, project, 1)
+    chi1 = st.stabilizer_rank
+    ms_norm, norm = _timed(torch, stream, st.norm, 1)
+    qargs = list(range(8, 16))
+    zs = []
+    for S in range(256):
+        ops = np.zeros(n, np.uint8)
+        for i in range(8):
+            if (S >> i) & 1:
+                ops[qargs[i]] = 3
+        zs.append(PauliString.dense(ops))
+    ms_mx, e_mx = _timed(torch, stream, lambda: st.exp_values(zs, PRECISION_MIXED), 1)
+    ms_64, e_64 = _timed(torch, stream, lambda: st.exp_values(zs, PRECISION_FP64), 1)
+
+    def marginal(e):
+        e = np.asarray(e, float).copy()
+        h = 1
+        while h < 256:
+            for i in range(0, 256, 2 * h):
+                a, b = e[i:i + h].copy(), e[i + h:i + 2 * h].copy()
+                e[i:i + h], e[i + h:i + 2 * h] = a + b, a - b
+            h *= 2
+        return np.maximum(e / (256.0 * e_64[0]), 0.0)
+    p64, pmx = marginal(e_64), marginal(e_mx)
+    shots = cfg["shots"]
+    ms_samp, (vals, cnts) = _timed(torch, stream, lambda: st.sample_raw(qargs, shots, seed=cfg["seed"]), 1)
+    clocks.stop()
+    hist = np.zeros(256)
+    for v, c in zip(vals, cnts):
+        hist[v] += c
+    tvd = 0.5 * float(np.abs(hist / shots - p64).sum())
+    line = {"metric": METRIC, "value": 256 / (ms_mx * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": 1,
+            "warmup": 0, "ms_per_step": ms_mx, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 accumulation of exact pair values, f64 final reduction", "data": "synthetic (seeded generator)",
+            "config": {"workload": "n=64, 8000 {H,S,CX} + 40 T (seed 5); project q0-7 onto seeded outcomes; "
+                                   "1e6 samples of q8-15", "outcomes_q0_7": outcomes, "chi_compiled": chi0,
+                       "chi_after_projection": chi1, "pairs_per_observable": chi1 * (chi1 + 1) // 2,
+                       "compile_s": compile_s, "l2": "inputs larger than L2"},
+            "stage_ms": {"project_and_renormalise": ms_proj, "norm_fp64": ms_norm,
+                         "z_strings_256_mixed": ms_mx, "z_strings_256_fp64": ms_64, "sample_1e6": ms_samp},
+            "norm_after_renormalise": norm, "norm_error": abs(norm - 1.0),
+            "marginal_max_abs_diff_mixed_vs_fp64": float(np.abs(pmx - p64).max()),
+            "tvd_samples_vs_fp64_marginal": tvd,
+            "tvd_expected_from_sampling_noise": 0.5 * float(np.sqrt(2.0 * p64 * (1 - p64) / (np.pi * shots)).sum()),
+            "clocks": clocks.summary()}
+    print(json.dumps(line))
+
+
+def run_workload(args):
+    torch, L = _setup_gpu()
+    {"precision60": run_precision60, "batch512": run_batch512,
+     "project64": run_project64}[args.workload](args, torch, L)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -312,11 +533,18 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--workload", default="plain40", choices=["plain40", "precision60", "batch512", "project64"],
+                    help="plain40: the headline line; the others measure the precision, batching and "
+                         "projection/sampling workloads (one JSON line each)")
+    ap.add_argument("--plain-circuits", type=int, default=512,
+                    help="batch512: circuits timed on the plain per-circuit path")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
-    else:
+    elif args.workload == "plain40":
         run_ours(args)
+    else:
+        run_workload(args)
 
 
 if __name__ == "__main__":

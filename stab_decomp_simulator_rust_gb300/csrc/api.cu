@@ -924,6 +924,58 @@ void sample_rec(nsg_state* s, const std::vector<std::pair<uint32_t, uint32_t>>& 
     }
 }
 
+// The marginal distribution of the qubits qs (processing order: bit i of x ↔
+// qs[i]) from one batched pass over every Z-string on them:
+// p(x) = 2^{-k}·Σ_S (-1)^{|x∧S|}·⟨Z_S⟩/⟨I⟩, a Walsh–Hadamard transform.
+std::vector<double> walsh_marginal(nsg_state* s, const std::vector<std::pair<uint32_t, uint32_t>>& qs) {
+    require_pairs_width(s);
+    const size_t k = qs.size(), N = (size_t)1 << k;
+    std::vector<DevPauli> ps(N, DevPauli{0, 0, 0, 0});
+    for (size_t S = 0; S < N; S++)
+        for (size_t i = 0; i < k; i++)
+            if ((S >> i) & 1) ps[S].pz |= 1ULL << qs[i].first;
+    std::vector<double> e;
+    run_pairs(s, s, ps, true, false, false, e);
+    const double norm2 = e[0];
+    for (size_t len = 1; len < N; len <<= 1)
+        for (size_t i = 0; i < N; i += 2 * len)
+            for (size_t j = i; j < i + len; j++) {
+                const double a = e[j], b = e[j + len];
+                e[j] = a + b;
+                e[j + len] = a - b;
+            }
+    for (size_t x = 0; x < N; x++) e[x] = (norm2 > 0.0) ? std::max(0.0, e[x] / ((double)N * norm2)) : 0.0;
+    return e;
+}
+
+// recursive_sample's binomial splitting (sampling.rs:80-189), same node order
+// and draws as sample_rec, with the branch weights read off the marginal.
+void sample_marginal(const std::vector<double>& p, const std::vector<std::pair<uint32_t, uint32_t>>& qs, size_t idx,
+                     uint32_t prefix, uint64_t shots, uint64_t lo, uint64_t hi, HostRng& rng, std::vector<ShotOut>& out) {
+    if (shots == 0) return;
+    if (idx == qs.size()) {
+        out.push_back({lo, hi, shots});
+        return;
+    }
+    const uint32_t low = (1u << idx) - 1;
+    double w0 = 0.0, w1 = 0.0;
+    for (size_t x = 0; x < p.size(); x++)
+        if ((x & low) == prefix) ((x >> idx) & 1 ? w1 : w0) += p[x];
+    const double tot = w0 + w1;
+    const double p0 = tot > 0 ? std::min(1.0, std::max(0.0, w0 / tot)) : 0.0;
+    const uint64_t n0 = rng.binomial(shots, p0), n1 = shots - n0;
+    sample_marginal(p, qs, idx + 1, prefix, n0, lo, hi, rng, out);
+    if (n1 > 0) {
+        const uint32_t bit = qs[idx].second;
+        uint64_t nlo = lo, nhi = hi;
+        if (bit < 64) nlo |= 1ULL << bit;
+        else nhi |= 1ULL << (bit - 64);
+        sample_marginal(p, qs, idx + 1, prefix | (1u << idx), n1, nlo, nhi, rng, out);
+    }
+}
+
+constexpr size_t kMarginalMaxQubits = 8;  // 2^8 Z-strings: one pair pass
+
 }  // namespace
 
 // ===========================================================================
@@ -1312,9 +1364,15 @@ nsg_status nsg_sample(const nsg_state* cstate, const uint32_t* qargs, size_t num
     std::vector<std::pair<uint32_t, uint32_t>> qs;  // (qarg, bit), descending qarg (sampling.rs:31-37)
     for (size_t i = 0; i < num_qargs; i++) qs.push_back({qargs[i], (uint32_t)i});
     std::stable_sort(qs.begin(), qs.end(), [](auto& a, auto& b) { return a.first > b.first; });
-    std::unique_ptr<nsg_state> work(clone_state(state));
     std::vector<ShotOut> res;
-    sample_rec(work.get(), qs, 0, shots, 0, 0, rng, res);
+    if (num_qargs <= kMarginalMaxQubits && state->t.n <= 64) {
+        // The node weights of the split tree all come from one marginal.
+        std::vector<double> p = walsh_marginal(state, qs);
+        sample_marginal(p, qs, 0, 0, shots, 0, 0, rng, res);
+    } else {
+        std::unique_ptr<nsg_state> work(clone_state(state));
+        sample_rec(work.get(), qs, 0, shots, 0, 0, rng, res);
+    }
     *num_out = res.size();
     if (res.size() > capacity)
         raise(NSG_ERR_BUFFER_TOO_SMALL, (int64_t)res.size(), (int64_t)capacity,

@@ -37,7 +37,7 @@ struct HostRng {
             w[0] = (uint64_t)std::chrono::high_resolution_clock::now().time_since_epoch().count();
             w[1] = (uint64_t)(uintptr_t)this;
         }
-        uint64_t x = w[0] ^ 0x243F6A8885A308D3ULL;
+        uint64_t x = 0x243F6A8885A308D3ULL;  // every seed word enters the chain once
         for (int i = 0; i < 4; i++) {
             x ^= w[i];
             s[i] = splitmix(x);

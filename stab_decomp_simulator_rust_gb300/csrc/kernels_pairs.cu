@@ -6,20 +6,26 @@
 // e^{iπk/4}·2^{-r/2} (or 0) — a canonical number, so any exact method gives
 // the reference's (k, r).  The reference computes it by Gauss-eliminating A
 // to |0^n⟩ (a recorded list of O(n²) gates, form/inner_product.rs:52-123)
-// and replaying that list on a clone of B.  Here the same quantity is
-// evaluated in A's frame with per-term precomputation:
+// and replaying that list on a clone of B.  Here the same quantity is an
+// exponential sum evaluated in A's frame:
 //
 //   |A⟩ = φ_A U_A U_{H,A}|s_A⟩,  V = U_A^{-1} (tableau precomputed per A)
-//   ⟨A|P|B⟩ = conj(φ_A)·μ_{A,P}·⟨x_{A,P}| U_{H,A}·(V·U_B)·U_{H,B}|s_B⟩·φ_B
+//   ⟨A|P|B⟩ = conj(φ_A)·μ_{A,P}·⟨x_{A,P}| U_{H,A}·D·U_{H,B}|s_B⟩·φ_B,  D = V·U_B
 //
 // with (x_{A,P}, μ_{A,P}) the Pauli seen from A's frame (precomputed per
-// (A, P)), V·U_B a product of two control-type Cliffords (one GF(2) matrix
-// pass), U_{H,A} applied with the reference's left_multiply_h rule, and the
-// final computational-basis amplitude in closed form (arXiv:1808.00128
-// eqs. 48-55).  One warp evaluates one pair with the tableau rows spread
-// over its lanes; the 32 lanes then evaluate up to 32 observables each
-// against the same transformed ket, so a batch of observables shares all of
-// the per-pair GF(2) work.
+// (A, P)).  D is control-type, so ⟨y|D U_{H,B}|s_B⟩ = ω^{ph_B}·2^{-|v_B|/2}·
+// i^{γ_D·y}·(-1)^{Q(y) + (yF_D)·(v_B∧s_B)}·δ((yF_D ⊕ s_B)∧¬v_B = 0) with
+// the quadratic form Q(y) = Σ_{p<r} y_p y_r K[r][p] + Σ_p y_p K[p][p],
+// K = M_D·F_Dᵀ (arXiv:1808.00128 eqs. 48-55).  ⟨x|U_{H,A} sums that over
+// the 2^{|v_A|} points y = x' ⊕ z, x' = x∧¬v_A, z ∈ span(v_A), which is a
+// sum of i^{L·z}·(-1)^{zᵀJz} under |¬v_B| linear constraints.  It is reduced
+// variable by variable (constraints by substitution, then each variable
+// summed out: an odd L_j gives √2·ω^{±1} and a rank-one update of J, an even
+// one gives 2·δ(linear form) and a substitution), O(n) steps of O(1) word
+// operations per lane.  The pivots, J and the low bits of L are the same for
+// every observable, so one warp reduces one pair for up to 256 observables
+// at once, each lane tracking the per-observable high bits of L, the phase
+// and the constraint right-hand sides of its observables.
 #include <cuda_runtime.h>
 
 #include <climits>
