@@ -62,6 +62,20 @@ def dist_env():
     return ws, rank, local
 
 
+def combine_ranks(ms_step: float, units_per_rank: int, device: str):
+    """Whole-job figures over replicas: the step time is the maximum over ranks
+    and the value counts the units of every rank (one replica per GPU, no
+    exchange on the data path)."""
+    ws, _, _ = dist_env()
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms_step], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    return ms_step, ws * units_per_rank / (ms_step * 1e-3)
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 class ClockSampler:
@@ -227,12 +241,7 @@ def run_ours(args):
     _ffi.check(L.nsg_profile_read(C.byref(pk_ms), C.byref(pk_launch), C.byref(pk_pairs)))
     _ffi.check(L.nsg_profile_enable(0))
     clocks.stop()
-    ms_step = total_ms / args.steps
-    if ws > 1:
-        t = torch.tensor([ms_step], device="cuda", dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = ws * nobs / (ms_step * 1e-3)
+    ms_step, value = combine_ranks(total_ms / args.steps, nobs, "cuda")
 
     # ---- mixed precision and the single-observable drop-in path
     for _ in range(2):
