@@ -399,8 +399,8 @@ def run_batch512(args, torch, L):
     Paulis each: every ⟨P⟩ of every circuit in one persistent launch per row
     width (nsg_exp_value_multi), against the plain path run per circuit and
     per observable (nsg_exp_value)."""
-    from stab_decomp_simulator_rust_gb300 import (PRECISION_FP64, PRECISION_MIXED, PauliString, QuantumState,
-                                                  exp_values_multi)
+    from stab_decomp_simulator_rust_gb300 import (PRECISION_FP64, PRECISION_MIXED, BatchPlan, PauliString,
+                                                  QuantumState, exp_values_multi)
     from stab_decomp_simulator_rust_gb300 import workloads as W
     circuits = W.batch_circuits()
     stream = torch.cuda.current_stream()
@@ -414,12 +414,17 @@ def run_batch512(args, torch, L):
     chis = [s.stabilizer_rank for s in states]
     pairs = sum(c * (c + 1) // 2 for c in chis)
     nobs = sum(len(p) for p in plists)
+    # the batched path as a captured plan (CUDA graph; kernel variant tuned on a sample at creation)
+    t0 = time.perf_counter()
+    plan = BatchPlan(states, plists, PRECISION_MIXED)
+    plan_s = time.perf_counter() - t0
     for _ in range(args.warmup):
-        exp_values_multi(states, plists, PRECISION_MIXED)
+        plan.run()
     torch.cuda.synchronize()
     clocks = ClockSampler(0)
     clocks.start()
-    msmx, vmx = _timed(torch, stream, lambda: exp_values_multi(states, plists, PRECISION_MIXED), args.steps)
+    msmx, vmx = _timed(torch, stream, plan.run, args.steps)
+    msdir, _ = _timed(torch, stream, lambda: exp_values_multi(states, plists, PRECISION_MIXED), 1)
     ms64, v64 = _timed(torch, stream, lambda: exp_values_multi(states, plists, PRECISION_FP64), args.steps)
     # plain: one circuit and one observable per call, FP64
     npl = min(args.plain_circuits, len(states))
@@ -427,8 +432,10 @@ def run_batch512(args, torch, L):
     def plain():
         return [[states[c].exp_value(p) for p in plists[c]] for c in range(npl)]
     mspl, vpl = _timed(torch, stream, plain, 1)
-    # the batched mixed path on the same circuits, for a like-for-like ratio
-    mssub, _ = _timed(torch, stream, lambda: exp_values_multi(states[:npl], plists[:npl], PRECISION_MIXED), 1)
+    # the batched mixed path (captured plan) on the same circuits, for a like-for-like ratio
+    sub = BatchPlan(states[:npl], plists[:npl], PRECISION_MIXED)
+    sub.run()
+    mssub, _ = _timed(torch, stream, sub.run, 1)
     clocks.stop()
     obs_pl = sum(len(plists[c]) for c in range(npl))
     err = np.concatenate([_rel_err(a, b) for a, b in zip(vmx, v64)])
@@ -449,6 +456,11 @@ def run_batch512(args, torch, L):
                        "observables": nobs, "l2": "inputs larger than L2 (term tables of 512 states)",
                        "compile_s_all_circuits": compile_s},
             "inner_products_per_s": sum(c * (c + 1) // 2 * len(p) for c, p in zip(chis, plists)) / (msmx * 1e-3),
+            "plan": {"create_s": plan_s, "tiling": plan.tiling,
+                     "path": "nsg_plan_run: CUDA-graph replay of frames, term tables, Pauli frames, pair launches, "
+                             "reductions and the result copy"},
+            "direct_batched_mixed": {"value": nobs / (msdir * 1e-3), "unit": UNIT, "ms": msdir,
+                                     "path": "nsg_exp_value_multi"},
             "fp64_batched": {"value": nobs / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64},
             "plain": {"value": obs_pl / (mspl * 1e-3), "unit": UNIT, "circuits": npl, "ms": mspl,
                       "path": "nsg_exp_value per circuit and observable, FP64"},

@@ -206,6 +206,31 @@ nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states
  * double. */
 nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pauli* pauli, double* out);
 
+/* A captured batched evaluation (no reference counterpart): the work of
+ * nsg_exp_value_multi — frames and term tables of every state, Pauli frames,
+ * the persistent pair launches, the reductions and the copy of the results
+ * to pinned host memory — captured once in a CUDA graph on the plan's own
+ * stream.  nsg_plan_run replays it and writes pauli_offsets[num_states]
+ * doubles to out.  Every run re-reads the states' current terms, so Clifford
+ * gates applied in place (nsg_apply_gates) are seen by the next run; an
+ * operation that changes a state's rank, width or global factor (projection,
+ * discard, measurement) or frees it makes nsg_plan_run fail with
+ * NSG_ERR_INVALID_ARGUMENT.  Creation picks the pair-kernel variant for each
+ * row width by timing the candidates on a sample of the plan's own work (one
+ * task per resident warp), remembered per device and workload class for the
+ * process; when the environment variable NSG_TUNE_CACHE names a file, the
+ * choices are also read from and appended to it (one JSON object per line). */
+typedef struct nsg_plan nsg_plan;
+nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, const nsg_pauli* paulis,
+                           const uint64_t* pauli_offsets, uint32_t precision, nsg_plan** out);
+nsg_status nsg_plan_run(nsg_plan* plan, double* out);
+/* The tiling in use: kets per chunk, tasks per resident warp, the kernel
+ * variant (blocks per SM its registers allow) for 32- and 64-bit rows, and
+ * whether creation timed candidates (1) or took them from the cache (0). */
+nsg_status nsg_plan_info(const nsg_plan* plan, int32_t* chunk, int32_t* tasks_per_warp, int32_t minb[2],
+                         int32_t* timed);
+void nsg_plan_free(nsg_plan* plan);
+
 /* QuantumState::inner_product ⟨a|b⟩ (crates/necstar/src/state/mod.rs:165-172 →
  * stabilizer_decomposed_state/inner_product.rs:9-19).  out = {re, im}. */
 nsg_status nsg_inner_product(const nsg_state* a, const nsg_state* b, double out[2]);

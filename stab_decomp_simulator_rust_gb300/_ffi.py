@@ -66,6 +66,11 @@ def load(path: str | None = None):
     L.nsg_exp_value_batch.argtypes = [vp, P(PauliABI), sz, u32, vp]
     L.nsg_exp_value_noalloc.argtypes = [vp, P(PauliABI), P(dbl)]
     L.nsg_exp_value_multi.argtypes = [vp, sz, P(PauliABI), vp, u32, vp]
+    L.nsg_plan_create.argtypes = [vp, sz, P(PauliABI), vp, u32, P(vp)]
+    L.nsg_plan_run.argtypes = [vp, vp]
+    L.nsg_plan_info.argtypes = [vp, P(i32), P(i32), vp, P(i32)]
+    L.nsg_plan_free.argtypes = [vp]
+    L.nsg_plan_free.restype = None
     L.nsg_inner_product.argtypes = [vp, vp, vp]
     L.nsg_norm.argtypes = [vp, P(dbl)]
     L.nsg_project_normalized.argtypes = [vp, u32, i32]
@@ -82,7 +87,7 @@ def load(path: str | None = None):
     L.nsg_probe_int_ops.argtypes = [u64, P(dbl), P(u64)]
     for name in header_symbols():
         fn = getattr(L, name)
-        if name not in ("nsg_version", "nsg_last_error_message", "nsg_state_free"):
+        if name not in ("nsg_version", "nsg_last_error_message", "nsg_state_free", "nsg_plan_free"):
             fn.restype = C.c_int32
     _lib = L
     return L

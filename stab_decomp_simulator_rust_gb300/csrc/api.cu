@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -396,12 +397,35 @@ DevPauli to_dev_pauli(const nsg_pauli& p, int n) {
 }  // namespace
 
 // ---------------------------------------------------------------------------
+// Live states by identity, so a plan can tell a freed (or replaced) state.
+static std::mutex g_states_mu;
+static std::map<const nsg_state*, uint64_t> g_states;
+static uint64_t g_next_uid = 1;
+
+static uint64_t register_state(const nsg_state* s) {
+    std::lock_guard<std::mutex> lk(g_states_mu);
+    const uint64_t id = g_next_uid++;
+    g_states[s] = id;
+    return id;
+}
+static void unregister_state(const nsg_state* s) {
+    std::lock_guard<std::mutex> lk(g_states_mu);
+    g_states.erase(s);
+}
+static bool state_alive(const nsg_state* s, uint64_t uid) {
+    std::lock_guard<std::mutex> lk(g_states_mu);
+    auto it = g_states.find(s);
+    return it != g_states.end() && it->second == uid;
+}
+
 struct nsg_state {
     int device = 0;
     cudaStream_t own = nullptr;
     cudaStream_t st = nullptr;
     TermStore t;
     double gf_re = 1.0, gf_im = 0.0;
+    uint64_t uid = 0;         // process-unique identity (plans check it)
+    uint64_t layout_gen = 0;  // bumped whenever the term storage is replaced or reshaped
     // cached bra frames
     bool frames_ok = false;
     DBuf<uint64_t> fGV, fFV, fMV, fGVL, fGVH;
@@ -420,6 +444,7 @@ struct nsg_state {
     }
 
     void init_stream() {
+        uid = register_state(this);
         CK(cudaGetDevice(&device));
         CK(cudaStreamCreateWithFlags(&own, cudaStreamNonBlocking));
         st = own;
@@ -429,6 +454,7 @@ struct nsg_state {
         CK(cudaMemsetAsync(status.p, 0, 8 * sizeof(int), st));
     }
     ~nsg_state() {
+        unregister_state(this);
         // Finish work on the current stream, then free everything on our own.
         if (st) cudaStreamSynchronize(st);
         t.rehome(own);
@@ -525,6 +551,7 @@ void compact_into(nsg_state* s, DBuf<int32_t>& keep) {
     CK(cudaStreamSynchronize(s->st));
     out.chi = h;
     s->t = std::move(out);
+    s->layout_gen++;
     s->invalidate();
 }
 
@@ -546,7 +573,6 @@ struct PairUnit {
     double* out = nullptr;  // host: nobs values, or nobs (re, im) pairs when complex_out
 };
 
-constexpr int kPairChunk = 32;       // kets per chunk (one ket-table prefetch chain)
 constexpr int kMaxObsPerUnit = 256;  // 8 observable groups of 32 lanes
 
 // Orders `st` after all work queued so far on `other`.
@@ -559,98 +585,106 @@ void join_stream(cudaStream_t st, cudaStream_t other) {
     cudaEventDestroy(ev);
 }
 
-// The batched Σ-pairs driver.  Every unit becomes one descriptor of a
-// persistent pair launch (one launch per word width: states of ≤ 32 qubits
-// run on 32-bit rows, wider ones on 64-bit rows), followed by one reduction
-// launch; all of it on `st`.  Bra frames and ket tables are built (once per
-// state, cached) on each state's own stream and joined into `st`.
-void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, uint8_t* dbg_k = nullptr,
-                    int32_t* dbg_r = nullptr) {
-    std::vector<PairUnit*> live;
-    for (auto& u : units) {
-        const size_t nout = (u.complex_out ? 2 : 1) * (size_t)u.nobs;
-        std::fill(u.out, u.out + nout, 0.0);
-        if (u.nobs > 0 && u.a->t.chi > 0 && u.b->t.chi > 0) live.push_back(&u);
-    }
-    if (live.empty()) return;
-    // Per-state caches on the states' streams, then join those streams.
-    std::vector<nsg_state*> touched;
-    for (PairUnit* u : live) {
-        u->a->frames();
-        u->a->ket_tables();
-        u->b->ket_tables();
-        touched.push_back(u->a);
-        touched.push_back(u->b);
-    }
-    std::sort(touched.begin(), touched.end());
-    touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
-    for (nsg_state* s : touched) join_stream(st, s->st);
+// Device sources of one unit: the bra state's frames and term tables and the
+// ket state's term tables (a state's own caches, or a plan's copies).
+struct UnitSources {
+    FrameView fr;
+    const void* atab = nullptr;
+    const void* ktab = nullptr;
+};
 
-    // Observables and Pauli frames of every unit.
-    size_t tot_obs = 0, tot_px = 0;
-    for (PairUnit* u : live) {
-        tot_obs += (size_t)u->nobs;
-        tot_px += (size_t)u->a->t.chi * u->nobs;
-    }
-    std::vector<DevPauli> hp;
-    hp.reserve(tot_obs);
-    for (PairUnit* u : live) hp.insert(hp.end(), u->paulis, u->paulis + u->nobs);
+// Tiling of a pair launch: kets per chunk, tasks per resident warp, and the
+// kernel variant (blocks per SM its registers allow) for 32- and 64-bit rows.
+struct PairTiling {
+    int chunk = 32;
+    int tasks_per_warp = 4;
+    int minb[2] = {4, 4};
+};
+
+// Everything one batched evaluation needs on the device, built once
+// (descriptors uploaded) and enqueued any number of times.
+struct PairBatch {
+    struct Launch {
+        int wb = 8;
+        MultiLaunch m;
+        DBuf<unsigned char> blob;  // descriptors | task_begin | obs_begin | row-chunk prefixes
+        DBuf<double> rec;          // task records, then the task counter
+        const int64_t* d_obegin = nullptr;
+        std::vector<int64_t> obegin;
+        std::vector<size_t> units;  // indices into `live`
+        size_t out_off = 0;         // first observable of this launch in `dout`
+        std::vector<int64_t> task_pairs;  // pairs covered by tasks [0, k) (prefix, for sampled timing)
+    };
+    std::vector<PairUnit*> live;
+    std::vector<UnitSources> src;
+    std::vector<size_t> unit_obs, unit_px, unit_out;  // per live unit
     DBuf<DevPauli> dp;
-    dp.alloc(tot_obs, st);
-    CK(cudaMemcpyAsync(dp.p, hp.data(), tot_obs * sizeof(DevPauli), cudaMemcpyHostToDevice, st));
     DBuf<uint64_t> px;
     DBuf<uint8_t> pk;
-    px.alloc(tot_px, st);
-    pk.alloc(tot_px, st);
+    std::vector<Launch> launches;
+    DBuf<double> dout;  // (re, im) per observable, launches concatenated
+    size_t tot_obs = 0;
+    uint64_t pairs = 0;
+};
 
-    bool prof;
-    {
-        std::lock_guard<std::mutex> lk(g_prof_mu);
-        prof = g_prof_on;
+void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st, uint8_t* dbg_k = nullptr,
+                 int32_t* dbg_r = nullptr) {
+    const size_t L = b.live.size();
+    b.tot_obs = 0;
+    size_t tot_px = 0;
+    b.unit_obs.assign(L, 0);
+    b.unit_px.assign(L, 0);
+    b.unit_out.assign(L, 0);
+    for (size_t k = 0; k < L; k++) {
+        b.unit_obs[k] = b.tot_obs;
+        b.unit_px[k] = tot_px;
+        b.tot_obs += (size_t)b.live[k]->nobs;
+        tot_px += (size_t)b.live[k]->a->t.chi * b.live[k]->nobs;
     }
-    std::vector<double> hout(2 * tot_obs, 0.0);
-    std::vector<DBuf<unsigned char>> keep_alive;  // per-launch descriptor buffers
-    std::vector<DBuf<double>> keep_rec;
-    float prof_ms = 0.f;
-    uint64_t prof_pairs = 0, prof_launches = 0;
-
-    size_t obs_base = 0, px_base = 0;
-    std::vector<size_t> unit_obs(live.size()), unit_px(live.size());
-    for (size_t k = 0; k < live.size(); k++) {
-        unit_obs[k] = obs_base;
-        unit_px[k] = px_base;
-        obs_base += (size_t)live[k]->nobs;
-        px_base += (size_t)live[k]->a->t.chi * live[k]->nobs;
-        CK(launch_pauli_frames(live[k]->a->t.view(), dp.p + unit_obs[k], live[k]->nobs, px.p + unit_px[k],
-                               pk.p + unit_px[k], st));
-    }
-
+    std::vector<DevPauli> hp;
+    hp.reserve(b.tot_obs);
+    for (PairUnit* u : b.live) hp.insert(hp.end(), u->paulis, u->paulis + u->nobs);
+    b.dp.alloc(std::max<size_t>(b.tot_obs, 1), st);
+    CK(cudaMemcpyAsync(b.dp.p, hp.data(), b.tot_obs * sizeof(DevPauli), cudaMemcpyHostToDevice, st));
+    b.px.alloc(std::max<size_t>(tot_px, 1), st);
+    b.pk.alloc(std::max<size_t>(tot_px, 1), st);
+    b.dout.alloc(2 * std::max<size_t>(b.tot_obs, 1), st);
+    b.launches.clear();
+    b.pairs = 0;
+    size_t out_base = 0;
     for (int wb : {4, 8}) {
         std::vector<size_t> sel;
-        for (size_t k = 0; k < live.size(); k++)
-            if ((live[k]->b->t.n <= 32 ? 4 : 8) == wb) sel.push_back(k);
+        for (size_t k = 0; k < L; k++)
+            if ((b.live[k]->b->t.n <= 32 ? 4 : 8) == wb) sel.push_back(k);
         if (sel.empty()) continue;
+        b.launches.emplace_back();
+        PairBatch::Launch& ln = b.launches.back();
+        ln.wb = wb;
+        ln.units = sel;
+        ln.out_off = out_base;
         // Host descriptors; row-chunk prefixes of the triangular units in one buffer.
         std::vector<PairDesc> descs(sel.size());
-        std::vector<int64_t> tbegin(sel.size() + 1, 0), obegin(sel.size() + 1, 0), offs;
+        std::vector<int64_t> tbegin(sel.size() + 1, 0), offs;
+        ln.obegin.assign(sel.size() + 1, 0);
         std::vector<size_t> off_at(sel.size(), 0);
         size_t tab_max = 0, bra_max = 0;
         int nobs_max = 1;
         for (size_t q = 0; q < sel.size(); q++) {
-            PairUnit* u = live[sel[q]];
+            PairUnit* u = b.live[sel[q]];
+            const UnitSources& s = b.src[sel[q]];
             const int64_t chiA = u->a->t.chi, chiB = u->b->t.chi;
             PairDesc& d = descs[q];
             d.A = u->a->t.view();
             d.B = u->b->t.view();
-            d.fr = u->a->frames();
-            d.ktab = u->b->ket_tables();
-            d.atab = u->a->ket_tables();
+            d.fr = s.fr;
+            d.ktab = s.ktab;
+            d.atab = s.atab;
             d.ktab_stride = ket_table_stride(u->b->t.n);
             d.ket_bytes = (uint32_t)ket_table_ket_bytes(u->b->t.n);
             d.ngrp = ket_table_groups(u->b->t.n);
             d.nobs = u->nobs;
-            d.px = px.p + unit_px[sel[q]];
-            d.pk = pk.p + unit_px[sel[q]];
+            d.px = b.px.p + b.unit_px[sel[q]];
+            d.pk = b.pk.p + b.unit_px[sel[q]];
             d.triangular = u->triangular ? 1 : 0;
             d.complex_out = u->complex_out ? 1 : 0;
             d.status = u->a->status.p;
@@ -667,31 +701,35 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
                 int64_t acc = 0;
                 for (int64_t i = 0; i < chiA; i++) {
                     offs.push_back(acc);
-                    acc += (chiA - i + kPairChunk - 1) / kPairChunk;
+                    acc += (chiA - i + tl.chunk - 1) / tl.chunk;
                 }
                 offs.push_back(acc);
                 nch = acc;
-                prof_pairs += (uint64_t)(chiA * (chiA + 1) / 2);
+                b.pairs += (uint64_t)(chiA * (chiA + 1) / 2);
             } else {
-                d.cpr = (chiB + kPairChunk - 1) / kPairChunk;
+                d.cpr = (chiB + tl.chunk - 1) / tl.chunk;
                 nch = chiA * d.cpr;
-                prof_pairs += (uint64_t)(chiA * chiB);
+                b.pairs += (uint64_t)(chiA * chiB);
             }
             d.nchunks = nch;
-            obegin[q + 1] = obegin[q] + u->nobs;
+            ln.obegin[q + 1] = ln.obegin[q] + u->nobs;
+            b.unit_out[sel[q]] = out_base + (size_t)ln.obegin[q];
             tab_max = std::max(tab_max, (size_t)d.ket_bytes);
             bra_max = std::max(bra_max, ket_table_bra_bytes(u->b->t.n));
             nobs_max = std::max(nobs_max, u->nobs);
         }
+        out_base += (size_t)ln.obegin.back();
         for (const PairDesc& d : descs)  // imaginary parts are accumulated with one observable group only
             if (d.complex_out && nobs_max > 32)
                 raise(NSG_ERR_INVALID_ARGUMENT, nobs_max, 32, "complex pair sums take at most 32 observables per launch");
-        // Tasks: about four per resident warp, never spanning two units.
+        // Tasks: about tasks_per_warp per resident warp, never spanning two units.
         const size_t warp_smem = pair_warp_smem_bytes(tab_max, bra_max, wb);
-        const int64_t resident = pair_resident_warps(wb, nobs_max, warp_smem);
+        const int minb = tl.minb[wb == 4 ? 0 : 1];
+        const int64_t resident = pair_resident_warps(wb, nobs_max, warp_smem, minb);
         int64_t total_chunks = 0;
         for (const PairDesc& d : descs) total_chunks += d.nchunks;
-        const int64_t task_chunks = std::max<int64_t>(1, (total_chunks + 4 * resident - 1) / (4 * resident));
+        const int64_t want = (int64_t)tl.tasks_per_warp * resident;
+        const int64_t task_chunks = std::max<int64_t>(1, (total_chunks + want - 1) / want);
         int64_t rec_doubles = 0;
         for (size_t q = 0; q < sel.size(); q++) {
             const int64_t nt = (descs[q].nchunks + task_chunks - 1) / task_chunks;
@@ -700,37 +738,64 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
             rec_doubles += nt * descs[q].nobs * 8;
         }
         const int64_t total_tasks = tbegin.back();
+        // Pairs covered by tasks [0, k) for the first tasks (two rounds of the
+        // grid), for timing samples: pairs before chunk c of unit q in closed form.
+        {
+            auto pairs_before = [&](size_t q, int64_t c) -> int64_t {
+                const PairUnit* u = b.live[sel[q]];
+                const int64_t chiA = u->a->t.chi, chiB = u->b->t.chi;
+                if (!u->triangular)
+                    return (c / descs[q].cpr) * chiB + std::min<int64_t>((c % descs[q].cpr) * tl.chunk, chiB);
+                const int64_t* off = offs.data() + off_at[q];
+                const int64_t i = (int64_t)(std::upper_bound(off, off + chiA + 1, c) - off) - 1;
+                if (i >= chiA) return chiA * (chiA + 1) / 2;
+                return i * chiA - i * (i - 1) / 2 + std::min<int64_t>((c - off[i]) * tl.chunk, chiA - i);
+            };
+            const int64_t lim = std::min<int64_t>(total_tasks, 2 * (int64_t)tl.tasks_per_warp * resident);
+            ln.task_pairs.assign((size_t)lim + 1, 0);
+            int64_t before = 0;  // pairs of the units before q
+            size_t q = 0;
+            for (int64_t k = 1; k <= lim; k++) {
+                while (k > tbegin[q + 1]) {
+                    before += pairs_before(q, descs[q].nchunks);
+                    q++;
+                }
+                ln.task_pairs[(size_t)k] =
+                    before + pairs_before(q, std::min<int64_t>((k - tbegin[q]) * task_chunks, descs[q].nchunks));
+            }
+        }
         // One buffer: descriptors | task_begin | obs_begin | row-chunk prefixes.
         const size_t b_desc = sel.size() * sizeof(PairDesc);
-        const size_t b_db = tbegin.size() * 8, b_ob = obegin.size() * 8, b_off = offs.size() * 8;
-        keep_alive.emplace_back();
-        DBuf<unsigned char>& blob = keep_alive.back();
-        blob.alloc(b_desc + b_db + b_ob + b_off, st);
-        int64_t* d_db = (int64_t*)(blob.p + b_desc);
-        int64_t* d_ob = (int64_t*)(blob.p + b_desc + b_db);
-        int64_t* d_off = (int64_t*)(blob.p + b_desc + b_db + b_ob);
+        const size_t b_db = tbegin.size() * 8, b_ob = ln.obegin.size() * 8, b_off = offs.size() * 8;
+        ln.blob.alloc(b_desc + b_db + b_ob + b_off, st);
+        int64_t* d_db = (int64_t*)(ln.blob.p + b_desc);
+        int64_t* d_ob = (int64_t*)(ln.blob.p + b_desc + b_db);
+        int64_t* d_off = (int64_t*)(ln.blob.p + b_desc + b_db + b_ob);
         for (size_t q = 0; q < sel.size(); q++)
             if (descs[q].triangular) descs[q].row_chunk_off = d_off + off_at[q];
         std::vector<unsigned char> hb(b_desc + b_db + b_ob + b_off);
         std::memcpy(hb.data(), descs.data(), b_desc);
         std::memcpy(hb.data() + b_desc, tbegin.data(), b_db);
-        std::memcpy(hb.data() + b_desc + b_db, obegin.data(), b_ob);
+        std::memcpy(hb.data() + b_desc + b_db, ln.obegin.data(), b_ob);
         if (b_off) std::memcpy(hb.data() + b_desc + b_db + b_ob, offs.data(), b_off);
-        CK(cudaMemcpyAsync(blob.p, hb.data(), hb.size(), cudaMemcpyHostToDevice, st));
+        // (a pageable source is staged before the call returns, so hb may go out of scope)
+        CK(cudaMemcpyAsync(ln.blob.p, hb.data(), hb.size(), cudaMemcpyHostToDevice, st));
+        ln.d_obegin = d_ob;
 
-        MultiLaunch m;
-        m.descs = (const PairDesc*)blob.p;
+        MultiLaunch& m = ln.m;
+        m.descs = (const PairDesc*)ln.blob.p;
         m.num_descs = (int)sel.size();
         m.task_begin = d_db;
         m.total_tasks = total_tasks;
         m.task_chunks = (int)task_chunks;
-        m.chunk = kPairChunk;
+        m.chunk = tl.chunk;
         m.nobs_max = nobs_max;
         m.mixed = mixed;
         const int wpb = 4;  // warps per block of the pair kernel
         const int64_t warps = std::min<int64_t>(total_tasks, resident);
         m.blocks = (int)std::max<int64_t>(1, (warps + wpb - 1) / wpb);
         m.nwarps = m.blocks * wpb;
+        m.minb = minb;
         m.tab_bytes_max = tab_max;
         m.bra_bytes_max = bra_max;
         m.warp_smem = warp_smem;
@@ -738,58 +803,121 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
             m.dbg_k = dbg_k;
             m.dbg_r = dbg_r;
         }
-        keep_rec.emplace_back();
-        DBuf<double>& rec = keep_rec.back();
-        rec.alloc((size_t)rec_doubles + 1, st);  // records, then the task counter
-        CK(cudaMemsetAsync(rec.p, 0, rec.n * sizeof(double), st));
-        m.records = rec.p;
-        m.counter = (unsigned long long*)(rec.p + rec_doubles);
+        ln.rec.alloc((size_t)rec_doubles + 1, st);  // records, then the task counter
+        m.records = ln.rec.p;
+        m.counter = (unsigned long long*)(ln.rec.p + rec_doubles);
+    }
+}
 
+// Enqueues the Pauli frames, the pair launches and the reductions of a built
+// batch on `st` (no host synchronisation).  With `max_tasks` > 0 only the first
+// tasks of each launch run (a timing sample; results are not meaningful).
+void enqueue_batch(PairBatch& b, cudaStream_t st, float* pair_ms = nullptr, int64_t max_tasks = 0) {
+    for (size_t k = 0; k < b.live.size(); k++)
+        CK(launch_pauli_frames(b.live[k]->a->t.view(), b.dp.p + b.unit_obs[k], b.live[k]->nobs,
+                               b.px.p + b.unit_px[k], b.pk.p + b.unit_px[k], st));
+    for (PairBatch::Launch& ln : b.launches) {
+        CK(cudaMemsetAsync(ln.rec.p, 0, ln.rec.n * sizeof(double), st));
+        MultiLaunch m = ln.m;
+        if (max_tasks > 0 && max_tasks < m.total_tasks) {
+            m.total_tasks = max_tasks;
+            const int64_t warps = std::min<int64_t>(max_tasks, (int64_t)m.nwarps);
+            m.blocks = (int)std::max<int64_t>(1, (warps + 3) / 4);
+            m.nwarps = m.blocks * 4;
+        }
         cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-        if (prof) {
+        if (pair_ms) {
             CK(cudaEventCreate(&ev0));
             CK(cudaEventCreate(&ev1));
             CK(cudaEventRecord(ev0, st));
         }
-        CK(launch_pairs_multi(m, wb, st));
-        if (prof) {
+        CK(launch_pairs_multi(m, ln.wb, st));
+        if (pair_ms) {
             CK(cudaEventRecord(ev1, st));
             CK(cudaEventSynchronize(ev1));
             float ms = 0.f;
             CK(cudaEventElapsedTime(&ms, ev0, ev1));
             cudaEventDestroy(ev0);
             cudaEventDestroy(ev1);
-            prof_ms += ms;
-            prof_launches += 1;
+            *pair_ms += ms;
         }
-        DBuf<double> lout;
-        lout.alloc(2 * (size_t)obegin.back(), st);
-        CK(launch_reduce_multi(m, d_ob, obegin.back(), lout.p, st));
-        std::vector<double> hl(2 * (size_t)obegin.back());
-        CK(cudaMemcpyAsync(hl.data(), lout.p, hl.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
-        CK(cudaStreamSynchronize(st));
-        for (size_t q = 0; q < sel.size(); q++)
-            std::memcpy(hout.data() + 2 * unit_obs[sel[q]], hl.data() + 2 * obegin[q],
-                        2 * (size_t)live[sel[q]]->nobs * sizeof(double));
+        CK(launch_reduce_multi(m, ln.d_obegin, ln.obegin.back(), b.dout.p + 2 * ln.out_off, st));
     }
-    if (prof) {
-        std::lock_guard<std::mutex> lk(g_prof_mu);
-        g_prof_ms += prof_ms;
-        g_prof_launches += prof_launches;
-        g_prof_pairs += prof_pairs;
-    }
-    CK(cudaStreamSynchronize(st));
-    for (size_t k = 0; k < live.size(); k++) {
-        PairUnit* u = live[k];
-        const double* r = hout.data() + 2 * unit_obs[k];
+}
+
+// Copies the (re, im) results (2 per observable, launch order) into the units.
+void scatter_batch(const PairBatch& b, const double* host) {
+    for (size_t k = 0; k < b.live.size(); k++) {
+        PairUnit* u = b.live[k];
+        const double* r = host + 2 * b.unit_out[k];
         if (u->complex_out) {
             std::memcpy(u->out, r, 2 * (size_t)u->nobs * sizeof(double));
         } else {
             for (int o = 0; o < u->nobs; o++) u->out[o] = r[2 * o];
         }
     }
+}
+
+std::vector<PairUnit*> live_units(std::vector<PairUnit>& units) {
+    std::vector<PairUnit*> live;
+    for (auto& u : units) {
+        const size_t nout = (u.complex_out ? 2 : 1) * (size_t)u.nobs;
+        std::fill(u.out, u.out + nout, 0.0);
+        if (u.nobs > 0 && u.a->t.chi > 0 && u.b->t.chi > 0) live.push_back(&u);
+    }
+    return live;
+}
+
+std::vector<nsg_state*> distinct_states(const std::vector<PairUnit*>& live) {
+    std::vector<nsg_state*> s;
+    for (PairUnit* u : live) {
+        s.push_back(u->a);
+        s.push_back(u->b);
+    }
+    std::sort(s.begin(), s.end());
+    s.erase(std::unique(s.begin(), s.end()), s.end());
+    return s;
+}
+
+// The batched Σ-pairs driver.  Every unit becomes one descriptor of a
+// persistent pair launch (one launch per word width: states of ≤ 32 qubits
+// run on 32-bit rows, wider ones on 64-bit rows), followed by one reduction
+// launch; all of it on `st`.  Bra frames and term tables are built (once per
+// state, cached) on each state's own stream and joined into `st`.
+void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, uint8_t* dbg_k = nullptr,
+                    int32_t* dbg_r = nullptr) {
+    PairBatch b;
+    b.live = live_units(units);
+    if (b.live.empty()) return;
+    for (PairUnit* u : b.live) {
+        UnitSources s;
+        s.fr = u->a->frames();
+        s.atab = u->a->ket_tables();
+        s.ktab = u->b->ket_tables();
+        b.src.push_back(s);
+    }
+    const std::vector<nsg_state*> touched = distinct_states(b.live);
+    for (nsg_state* s : touched) join_stream(st, s->st);
+    build_batch(b, PairTiling(), mixed, st, dbg_k, dbg_r);
+    bool prof;
+    {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        prof = g_prof_on;
+    }
+    float prof_ms = 0.f;
+    enqueue_batch(b, st, prof ? &prof_ms : nullptr);
+    std::vector<double> hout(2 * b.tot_obs);
+    CK(cudaMemcpyAsync(hout.data(), b.dout.p, hout.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (prof) {
+        std::lock_guard<std::mutex> lk(g_prof_mu);
+        g_prof_ms += prof_ms;
+        g_prof_launches += b.launches.size();
+        g_prof_pairs += b.pairs;
+    }
+    scatter_batch(b, hout.data());
     // The launches ran on `st`; each bra state's status words report its units.
-    for (size_t k = 0; k < touched.size(); k++) touched[k]->check_status();
+    for (nsg_state* s : touched) s->check_status();
 }
 
 // Σ-pairs of one (a, b) for any number of observables (split into units of
@@ -846,6 +974,7 @@ void discard_q(nsg_state* s, uint32_t q) {  // discard.rs:5-12
     CK(launch_discard(s->t.view(), (int)q, s->status.p, s->st));
     s->check_status(q);
     s->t.n -= 1;
+    s->layout_gen++;
     s->invalidate();
 }
 
@@ -976,7 +1105,158 @@ void sample_marginal(const std::vector<double>& p, const std::vector<std::pair<u
 
 constexpr size_t kMarginalMaxQubits = 8;  // 2^8 Z-strings: one pair pass
 
+// ---- tuning of captured batches ----------------------------------------------
+// The kernel variant (blocks per SM its registers allow) that ran fastest on a
+// sample, per device and workload class; also appended to the file named by
+// NSG_TUNE_CACHE, one JSON object per line: {"key": "...", "minb": k}.
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tune;
+bool g_tune_loaded = false;
+constexpr int kMinbCandidates[4] = {2, 3, 4, 5};
+
+std::string tune_key(int device, int wb, int nobs_max, int n_mean, uint64_t pairs) {
+    cudaDeviceProp prop;
+    std::string name = "gpu";
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) name = prop.name;
+    for (char& c : name)
+        if (c == '"' || c == '\\' || c == ' ') c = '_';
+    int lg = 0;
+    while ((pairs >> lg) > 1) lg++;
+    char buf[256];
+    std::snprintf(buf, sizeof(buf), "%s|w%d|g%d|n%d|p%d", name.c_str(), wb * 8, (nobs_max + 31) / 32,
+                  (n_mean + 7) / 8 * 8, lg / 2 * 2);
+    return buf;
+}
+
+void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = std::getenv("NSG_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    char line[512];
+    while (std::fgets(line, sizeof(line), f)) {
+        char key[256];
+        int minb = 0;
+        if (std::sscanf(line, " {\"key\": \"%255[^\"]\", \"minb\": %d}", key, &minb) == 2 && minb >= 2 && minb <= 5)
+            g_tune[key] = minb;
+    }
+    std::fclose(f);
+}
+
+bool tune_lookup(const std::string& key, int& minb) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked();
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) return false;
+    minb = it->second;
+    return true;
+}
+
+void tune_store(const std::string& key, int minb) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked();
+    g_tune[key] = minb;
+    const char* path = std::getenv("NSG_TUNE_CACHE");
+    if (!path || !*path) return;
+    if (FILE* f = std::fopen(path, "a")) {
+        std::fprintf(f, "{\"key\": \"%s\", \"minb\": %d}\n", key.c_str(), minb);
+        std::fclose(f);
+    }
+}
+
+// Device time per pair of one launch of a built batch, on a sample: one task
+// per resident warp (records and counter cleared first).
+double sample_ns_per_pair(PairBatch& b, size_t li, cudaStream_t st) {
+    PairBatch::Launch& ln = b.launches[li];
+    MultiLaunch m = ln.m;
+    const int64_t k = std::min<int64_t>(m.total_tasks, (int64_t)m.nwarps);
+    m.total_tasks = k;
+    CK(cudaMemsetAsync(ln.rec.p, 0, ln.rec.n * sizeof(double), st));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, st));
+    CK(launch_pairs_multi(m, ln.wb, st));
+    CK(cudaEventRecord(e1, st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    const int64_t pairs = ln.task_pairs.size() > (size_t)k ? ln.task_pairs[(size_t)k] : 0;
+    return pairs > 0 ? 1e6 * ms / (double)pairs : 1e300;
+}
+
 }  // namespace
+
+// ---------------------------------------------------------------------------
+// A plan's copy of one state's derived data and the identity it was built on.
+struct PlanState {
+    nsg_state* s = nullptr;
+    uint64_t uid = 0, gen = 0;
+    int n = 0;
+    int64_t chi = 0;
+    double gf_re = 1.0, gf_im = 0.0;
+    DBuf<uint64_t> gv, fv, mv, gvl, gvh;
+    DBuf<unsigned char> tab;
+    FrameView frames() const { return FrameView{gv.p, fv.p, mv.p, gvl.p, gvh.p}; }
+};
+
+struct nsg_plan {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<std::unique_ptr<PlanState>> states;
+    std::vector<DevPauli> paulis;
+    std::vector<PairUnit> units;
+    std::vector<double> results;  // one per observable, in the caller's order
+    PairBatch batch;
+    double* pinned = nullptr;
+    PairTiling tiling;
+    bool timed = false;
+
+    ~nsg_plan() {
+        if (st) cudaStreamSynchronize(st);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (pinned) cudaFreeHost(pinned);
+        batch = PairBatch();  // device buffers are freed on the plan's stream
+        states.clear();
+        if (st) {
+            cudaStreamSynchronize(st);
+            cudaStreamDestroy(st);
+        }
+    }
+    // Frames and term tables of every state, from their current terms.
+    void enqueue_derived() {
+        for (auto& ps : states) {
+            if (ps->chi == 0) continue;
+            CK(launch_frames(ps->s->t.view(), ps->frames(), st));
+            CK(launch_ket_tables(ps->s->t.view(), ps->tab.p, st));
+        }
+    }
+    PlanState* find(const nsg_state* s) {
+        for (auto& ps : states)
+            if (ps->s == s) return ps.get();
+        return nullptr;
+    }
+    void build(PairBatch& b, const PairTiling& tl, bool mixed) {
+        b.live = live_units(units);
+        b.src.clear();
+        for (PairUnit* u : b.live) {
+            UnitSources src;
+            src.fr = find(u->a)->frames();
+            src.atab = find(u->a)->tab.p;
+            src.ktab = find(u->b)->tab.p;
+            b.src.push_back(src);
+        }
+        build_batch(b, tl, mixed, st);
+    }
+};
+
 
 // ===========================================================================
 extern "C" {
@@ -1253,6 +1533,184 @@ nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states
     }
     API_END
 }
+
+nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, const nsg_pauli* paulis,
+                           const uint64_t* pauli_offsets, uint32_t precision, nsg_plan** out) {
+    API_BEGIN
+    need(out, "out");
+    *out = nullptr;
+    need(pauli_offsets, "pauli_offsets");
+    if (num_states) need(states, "states");
+    if (precision > NSG_PRECISION_MIXED) raise(NSG_ERR_INVALID_ARGUMENT, precision, -1, "invalid precision");
+    if (pauli_offsets[0] != 0) raise(NSG_ERR_INVALID_ARGUMENT, (int64_t)pauli_offsets[0], -1, "pauli_offsets[0] must be 0");
+    for (size_t c = 0; c < num_states; c++) {
+        need(states[c], "state");
+        if (pauli_offsets[c + 1] < pauli_offsets[c])
+            raise(NSG_ERR_INVALID_ARGUMENT, (int64_t)c, -1, "pauli_offsets not ascending at %zu", c);
+        require_pairs_width(states[c]);
+        if (states[c]->device != states[0]->device)
+            raise(NSG_ERR_INVALID_ARGUMENT, states[c]->device, states[0]->device, "all states must live on one device");
+    }
+    const uint64_t total = num_states ? pauli_offsets[num_states] : 0;
+    if (total) need(paulis, "paulis");
+    const bool mixed = precision == NSG_PRECISION_MIXED;
+    auto plan = std::make_unique<nsg_plan>();
+    plan->device = num_states ? states[0]->device : 0;
+    CK(cudaSetDevice(plan->device));
+    CK(cudaStreamCreateWithFlags(&plan->st, cudaStreamNonBlocking));
+    cudaStream_t st = plan->st;
+    plan->paulis.resize(total);
+    for (size_t c = 0; c < num_states; c++)
+        for (uint64_t k = pauli_offsets[c]; k < pauli_offsets[c + 1]; k++)
+            plan->paulis[k] = to_dev_pauli(paulis[k], states[c]->t.n);
+    plan->results.assign(total, 0.0);
+    // Each distinct state: its identity and the plan's own frames and term tables.
+    for (size_t c = 0; c < num_states; c++) {
+        nsg_state* s = const_cast<nsg_state*>(states[c]);
+        if (plan->find(s)) continue;
+        auto ps = std::make_unique<PlanState>();
+        ps->s = s;
+        ps->uid = s->uid;
+        ps->gen = s->layout_gen;
+        ps->n = s->t.n;
+        ps->chi = s->t.chi;
+        ps->gf_re = s->gf_re;
+        ps->gf_im = s->gf_im;
+        const size_t cap = (size_t)std::max<int64_t>(s->t.chi, 1);
+        ps->gv.alloc(cap * 64, st);
+        ps->fv.alloc(cap * 64, st);
+        ps->mv.alloc(cap * 64, st);
+        ps->gvl.alloc(cap, st);
+        ps->gvh.alloc(cap, st);
+        ps->tab.alloc(cap * ket_table_stride(s->t.n), st);
+        join_stream(st, s->st);
+        plan->states.push_back(std::move(ps));
+    }
+    for (size_t c = 0; c < num_states; c++) {
+        nsg_state* s = const_cast<nsg_state*>(states[c]);
+        for (uint64_t base = pauli_offsets[c]; base < pauli_offsets[c + 1]; base += kMaxObsPerUnit) {
+            PairUnit u;
+            u.a = s;
+            u.b = s;
+            u.paulis = plan->paulis.data() + base;
+            u.nobs = (int)std::min<uint64_t>(kMaxObsPerUnit, pauli_offsets[c + 1] - base);
+            u.out = plan->results.data() + base;
+            plan->units.push_back(u);
+        }
+    }
+    plan->enqueue_derived();
+
+    // Tiling: the kernel variant per row width, from the cache or timed on a sample.
+    PairTiling tl;
+    {
+        PairBatch probe;
+        plan->build(probe, tl, mixed);
+        std::vector<std::string> keys(2);
+        bool need_time[2] = {false, false};
+        for (const PairBatch::Launch& ln : probe.launches) {
+            const int idx = ln.wb == 4 ? 0 : 1;
+            uint64_t pairs = 0, nsum = 0;
+            for (size_t q : ln.units) {
+                const int64_t chi = probe.live[q]->a->t.chi;
+                pairs += (uint64_t)(chi * (chi + 1) / 2);
+                nsum += (uint64_t)probe.live[q]->a->t.n * (uint64_t)(chi * (chi + 1) / 2);
+            }
+            keys[idx] = tune_key(plan->device, ln.wb, ln.m.nobs_max, pairs ? (int)(nsum / pairs) : 0, pairs);
+            int minb = 4;
+            if (tune_lookup(keys[idx], minb)) tl.minb[idx] = minb;
+            else need_time[idx] = true;
+        }
+        if (need_time[0] || need_time[1]) {
+            plan->timed = true;
+            double best[2] = {1e300, 1e300};
+            int pick[2] = {tl.minb[0], tl.minb[1]};
+            for (int cand : kMinbCandidates) {
+                PairTiling tc = tl;
+                for (int idx = 0; idx < 2; idx++)
+                    if (need_time[idx]) tc.minb[idx] = cand;
+                PairBatch b;
+                plan->build(b, tc, mixed);
+                for (size_t k = 0; k < b.live.size(); k++)
+                    CK(launch_pauli_frames(b.live[k]->a->t.view(), b.dp.p + b.unit_obs[k], b.live[k]->nobs,
+                                           b.px.p + b.unit_px[k], b.pk.p + b.unit_px[k], st));
+                for (size_t li = 0; li < b.launches.size(); li++) {
+                    const int idx = b.launches[li].wb == 4 ? 0 : 1;
+                    if (!need_time[idx]) continue;
+                    sample_ns_per_pair(b, li, st);  // first launch of the variant: warm-up
+                    const double ns = sample_ns_per_pair(b, li, st);
+                    if (ns < best[idx]) {
+                        best[idx] = ns;
+                        pick[idx] = cand;
+                    }
+                }
+                CK(cudaStreamSynchronize(st));
+            }
+            for (int idx = 0; idx < 2; idx++)
+                if (need_time[idx]) {
+                    tl.minb[idx] = pick[idx];
+                    tune_store(keys[idx], pick[idx]);
+                }
+        }
+    }
+    plan->tiling = tl;
+    plan->build(plan->batch, tl, mixed);
+    const size_t nres = 2 * std::max<size_t>(plan->batch.tot_obs, 1);
+    CK(cudaMallocHost(&plan->pinned, nres * sizeof(double)));
+    if (!plan->batch.live.empty()) {
+        // One uncaptured run (checks the launches), then the capture.
+        enqueue_batch(plan->batch, st);
+        CK(cudaStreamSynchronize(st));
+        CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        plan->enqueue_derived();
+        enqueue_batch(plan->batch, st);
+        CK(cudaMemcpyAsync(plan->pinned, plan->batch.dout.p, 2 * plan->batch.tot_obs * sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamEndCapture(st, &plan->graph));
+        CK(cudaGraphInstantiate(&plan->exec, plan->graph, 0));
+    }
+    for (auto& ps : plan->states) ps->s->check_status();
+    *out = plan.release();
+    API_END
+}
+
+nsg_status nsg_plan_run(nsg_plan* plan, double* out) {
+    API_BEGIN
+    need(plan, "plan");
+    for (auto& ps : plan->states) {
+        const nsg_state* s = ps->s;
+        if (!state_alive(s, ps->uid) || s->layout_gen != ps->gen || s->t.n != ps->n || s->t.chi != ps->chi ||
+            s->gf_re != ps->gf_re || s->gf_im != ps->gf_im)
+            raise(NSG_ERR_INVALID_ARGUMENT, -1, -1,
+                  "a state of the plan was freed or changed its rank, width or global factor; create a new plan");
+    }
+    if (!plan->results.empty()) need(out, "out");
+    if (plan->exec) {
+        CK(cudaSetDevice(plan->device));
+        for (auto& ps : plan->states) join_stream(plan->st, ps->s->st);
+        CK(cudaGraphLaunch(plan->exec, plan->st));
+        CK(cudaStreamSynchronize(plan->st));
+        scatter_batch(plan->batch, plan->pinned);
+        for (auto& ps : plan->states) ps->s->check_status();
+    }
+    if (!plan->results.empty()) std::memcpy(out, plan->results.data(), plan->results.size() * sizeof(double));
+    API_END
+}
+
+nsg_status nsg_plan_info(const nsg_plan* plan, int32_t* chunk, int32_t* tasks_per_warp, int32_t minb[2],
+                         int32_t* timed) {
+    API_BEGIN
+    need(plan, "plan");
+    if (chunk) *chunk = plan->tiling.chunk;
+    if (tasks_per_warp) *tasks_per_warp = plan->tiling.tasks_per_warp;
+    if (minb) {
+        minb[0] = plan->tiling.minb[0];
+        minb[1] = plan->tiling.minb[1];
+    }
+    if (timed) *timed = plan->timed ? 1 : 0;
+    API_END
+}
+
+void nsg_plan_free(nsg_plan* plan) { delete plan; }
 
 nsg_status nsg_inner_product(const nsg_state* a, const nsg_state* b, double out[2]) {
     API_BEGIN

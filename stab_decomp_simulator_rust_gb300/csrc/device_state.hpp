@@ -179,6 +179,7 @@ struct MultiLaunch {
     unsigned long long* counter = nullptr;  // zero before the launch
     int nwarps = 0;
     int blocks = 0;
+    int minb = 4;                         // kernel variant: blocks per SM its registers allow (2..5)
     size_t tab_bytes_max = 0;             // largest ket_bytes among the units
     size_t bra_bytes_max = 0;             // largest bra (G) table among the units
     size_t warp_smem = 0;
@@ -195,7 +196,7 @@ cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, 
                                 cudaStream_t st);
 size_t pair_warp_smem_bytes(size_t ket_bytes_max, size_t bra_bytes_max, int word_bytes);
 // Warps of the pair kernel resident on the whole device at once.
-int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem);
+int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem, int minb);
 
 // The same sums with B's rows staged per pair instead of ket tables (no
 // per-term table storage; at most 32 observables).

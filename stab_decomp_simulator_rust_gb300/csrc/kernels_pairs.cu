@@ -470,8 +470,11 @@ __device__ __forceinline__ void g_subst(int kq, Word lp, const bool (&c)[NG], Wo
     if (lowk) g_expand<Word, RPL>(J, hs, L0, lp, own);
 }
 
-template <typename Word, int RPL, int NG>
-__global__ void __launch_bounds__(PWARPS * 32, 4) pair_kernel(MultiLaunch p) {
+// MINB: blocks per SM the register allocation must allow (the register cap is
+// 65536 / (128·MINB)); the launch picks it per workload (fewer blocks leave
+// more registers for many observables per lane).
+template <typename Word, int RPL, int NG, int MINB>
+__global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) {
     constexpr int GMAX = (8 * sizeof(Word)) / 4;  // groups of four rows (8 or 16)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1130,48 +1133,75 @@ __global__ void reduce_kernel(const double* __restrict__ partials, int nwarps, i
     }
 }
 
-// Dynamic shared memory above 48 KB needs an opt-in per kernel (and device).
-template <typename Word, int RPL, int NG>
-cudaError_t allow_smem(size_t smem) {
+// Dynamic shared memory above 48 KB needs an opt-in per kernel (and device);
+// it is set outside stream capture (the first launch of a shape is never a
+// captured one: plans run once before they capture).
+template <typename Word, int RPL, int NG, int MINB>
+cudaError_t allow_smem(size_t smem, cudaStream_t st) {
     if (smem <= 48 * 1024) return cudaSuccess;
-    return cudaFuncSetAttribute(pair_kernel<Word, RPL, NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (st) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) return cudaSuccess;
+    }
+    return cudaFuncSetAttribute(pair_kernel<Word, RPL, NG, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem);
 }
 
-template <typename Word, int RPL, int NG>
+template <typename Word, int RPL, int NG, int MINB>
 cudaError_t launch_pairs_ng(const MultiLaunch& p, cudaStream_t st) {
     const size_t smem = (size_t)p.warp_smem * PWARPS;
-    cudaError_t e = allow_smem<Word, RPL, NG>(smem);
+    cudaError_t e = allow_smem<Word, RPL, NG, MINB>(smem, st);
     if (e != cudaSuccess) return e;
-    pair_kernel<Word, RPL, NG><<<p.blocks, PWARPS * 32, smem, st>>>(p);
+    pair_kernel<Word, RPL, NG, MINB><<<p.blocks, PWARPS * 32, smem, st>>>(p);
     return cudaGetLastError();
 }
 
 template <typename Word, int RPL, int NG>
+cudaError_t launch_pairs_minb(const MultiLaunch& p, cudaStream_t st) {
+    switch (p.minb) {
+        case 2: return launch_pairs_ng<Word, RPL, NG, 2>(p, st);
+        case 3: return launch_pairs_ng<Word, RPL, NG, 3>(p, st);
+        case 5: return launch_pairs_ng<Word, RPL, NG, 5>(p, st);
+        default: return launch_pairs_ng<Word, RPL, NG, 4>(p, st);
+    }
+}
+
+template <typename Word, int RPL, int NG, int MINB>
 int resident_blocks_ng(size_t warp_smem) {
     int nb = 0;
-    if (allow_smem<Word, RPL, NG>(warp_smem * PWARPS) != cudaSuccess) return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pair_kernel<Word, RPL, NG>, PWARPS * 32,
+    if (allow_smem<Word, RPL, NG, MINB>(warp_smem * PWARPS, nullptr) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pair_kernel<Word, RPL, NG, MINB>, PWARPS * 32,
                                                       warp_smem * PWARPS) != cudaSuccess)
         return 1;
     return nb > 0 ? nb : 1;
 }
 
+template <typename Word, int RPL, int NG>
+int resident_blocks_minb(size_t warp_smem, int minb) {
+    switch (minb) {
+        case 2: return resident_blocks_ng<Word, RPL, NG, 2>(warp_smem);
+        case 3: return resident_blocks_ng<Word, RPL, NG, 3>(warp_smem);
+        case 5: return resident_blocks_ng<Word, RPL, NG, 5>(warp_smem);
+        default: return resident_blocks_ng<Word, RPL, NG, 4>(warp_smem);
+    }
+}
+
 template <typename Word, int RPL>
-int resident_blocks_w(int nobs_max, size_t warp_smem) {
+int resident_blocks_w(int nobs_max, size_t warp_smem, int minb) {
     const int ng = (nobs_max + 31) / 32;
-    if (ng <= 1) return resident_blocks_ng<Word, RPL, 1>(warp_smem);
-    if (ng <= 2) return resident_blocks_ng<Word, RPL, 2>(warp_smem);
-    if (ng <= 4) return resident_blocks_ng<Word, RPL, 4>(warp_smem);
-    return resident_blocks_ng<Word, RPL, 8>(warp_smem);
+    if (ng <= 1) return resident_blocks_minb<Word, RPL, 1>(warp_smem, minb);
+    if (ng <= 2) return resident_blocks_minb<Word, RPL, 2>(warp_smem, minb);
+    if (ng <= 4) return resident_blocks_minb<Word, RPL, 4>(warp_smem, minb);
+    return resident_blocks_minb<Word, RPL, 8>(warp_smem, minb);
 }
 
 template <typename Word, int RPL>
 cudaError_t launch_pairs_w(const MultiLaunch& p, cudaStream_t st) {
     const int ng = (p.nobs_max + 31) / 32;
-    if (ng <= 1) return launch_pairs_ng<Word, RPL, 1>(p, st);
-    if (ng <= 2) return launch_pairs_ng<Word, RPL, 2>(p, st);
-    if (ng <= 4) return launch_pairs_ng<Word, RPL, 4>(p, st);
-    if (ng <= 8) return launch_pairs_ng<Word, RPL, 8>(p, st);
+    if (ng <= 1) return launch_pairs_minb<Word, RPL, 1>(p, st);
+    if (ng <= 2) return launch_pairs_minb<Word, RPL, 2>(p, st);
+    if (ng <= 4) return launch_pairs_minb<Word, RPL, 4>(p, st);
+    if (ng <= 8) return launch_pairs_minb<Word, RPL, 8>(p, st);
     return cudaErrorInvalidValue;
 }
 
@@ -1262,9 +1292,9 @@ cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_
     return launch_pairs_w<uint64_t, 2>(m, st);
 }
 
-int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem) {
-    const int nb = word_bytes == 4 ? resident_blocks_w<uint32_t, 1>(nobs_max, warp_smem)
-                                   : resident_blocks_w<uint64_t, 2>(nobs_max, warp_smem);
+int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem, int minb) {
+    const int nb = word_bytes == 4 ? resident_blocks_w<uint32_t, 1>(nobs_max, warp_smem, minb)
+                                   : resident_blocks_w<uint64_t, 2>(nobs_max, warp_smem, minb);
     return nb * PWARPS * device_sm_count();
 }
 

@@ -239,11 +239,7 @@ class QuantumState:
         return d
 
 
-def exp_values_multi(states, paulis_per_state, precision: int = PRECISION_FP64) -> list[np.ndarray]:
-    """⟨P⟩ for many states at once: observables ``paulis_per_state[c]`` on
-    ``states[c]``, every pair sum in one persistent launch (one per row width:
-    ≤ 32 and > 32 qubits).  Returns one array per state, each value as
-    ``states[c].exp_values(paulis_per_state[c], precision)`` gives it."""
+def _multi_args(states, paulis_per_state):
     states = list(states)
     groups = [list(g) for g in paulis_per_state]
     if len(groups) != len(states):
@@ -259,6 +255,56 @@ def exp_values_multi(states, paulis_per_state, precision: int = PRECISION_FP64) 
             arr[k] = p.abi()
             k += 1
     hs = (C.c_void_p * max(len(states), 1))(*[s._h for s in states])
+    return states, groups, offs, total, arr, hs
+
+
+class BatchPlan:
+    """A captured batched evaluation (nsg_plan_*): the work of
+    ``exp_values_multi`` recorded once in a CUDA graph and replayed by
+    ``run()``.  Each run reads the states' current terms, so gates applied in
+    place are seen; projection, discard, measurement or freeing a state makes
+    ``run()`` raise.  Creation picks the pair-kernel variant by timing it on a
+    sample of the plan's work (or takes it from the tuning cache)."""
+
+    def __init__(self, states, paulis_per_state, precision: int = PRECISION_FP64):
+        states, groups, offs, total, arr, hs = _multi_args(states, paulis_per_state)
+        self._states = states  # keep the handles alive as long as the plan
+        self._groups = groups  # and the Pauli storage the ABI structs point into
+        self._offs = offs
+        self._out = np.zeros(max(total, 1), np.float64)
+        h = C.c_void_p()
+        check(_ffi.load().nsg_plan_create(hs, len(states), arr, _p(offs), precision, C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _ffi.load().nsg_plan_free(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def run(self) -> list[np.ndarray]:
+        check(_ffi.load().nsg_plan_run(self._h, _p(self._out)))
+        o = self._offs
+        return [self._out[int(o[c]):int(o[c + 1])].copy() for c in range(len(self._states))]
+
+    @property
+    def tiling(self) -> dict:
+        chunk, tpw, timed = C.c_int32(), C.c_int32(), C.c_int32()
+        minb = (C.c_int32 * 2)()
+        check(_ffi.load().nsg_plan_info(self._h, C.byref(chunk), C.byref(tpw), minb, C.byref(timed)))
+        return {"chunk": chunk.value, "tasks_per_warp": tpw.value, "minb_rows32": minb[0], "minb_rows64": minb[1],
+                "timed": bool(timed.value)}
+
+
+def exp_values_multi(states, paulis_per_state, precision: int = PRECISION_FP64) -> list[np.ndarray]:
+    """⟨P⟩ for many states at once: observables ``paulis_per_state[c]`` on
+    ``states[c]``, every pair sum in one persistent launch (one per row width:
+    ≤ 32 and > 32 qubits).  Returns one array per state, each value as
+    ``states[c].exp_values(paulis_per_state[c], precision)`` gives it."""
+    states, groups, offs, total, arr, hs = _multi_args(states, paulis_per_state)
     out = np.zeros(max(total, 1), np.float64)
     check(_ffi.load().nsg_exp_value_multi(hs, len(states), arr, _p(offs), precision, _p(out)))
     return [out[int(offs[c]):int(offs[c + 1])].copy() for c in range(len(states))]
