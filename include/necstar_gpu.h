@@ -316,6 +316,12 @@ nsg_status nsg_probe_int_ops(uint64_t iters, double* seconds, uint64_t* ops);
  * (crates/stabilizer-ch-form-rust/src/form/inner_product.rs:14-48) when
  * exp_value evaluates S_i against P·S_j (exp_value.rs:38-57).  Evaluates the
  * full χ×χ square with the production pair kernel; for parity tests. */
+/* The device expansion of |T⟩^{⊗t} (construct_t_tensor_state,
+ * crates/necstar/src/state/magic_states/t_state.rs:29-71; 1 ≤ t ≤ 64) as a
+ * state of t qubits whose terms and coefficients are the expansion's, in its
+ * order — for parity tests against the oracle. */
+nsg_status nsg_debug_t_tensor(uint32_t t, nsg_state** out);
+
 nsg_status nsg_debug_pair_values(const nsg_state* state, const nsg_pauli* pauli,
                                  uint8_t* k, int32_t* r);
 

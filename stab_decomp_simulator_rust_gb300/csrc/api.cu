@@ -189,14 +189,6 @@ struct TermStore {
 
 // ---------------------------------------------------------------------------
 // |T⟩^{⊗t} expansion, cached per t (host) and per (device, t) (device).
-struct TTensorHost {
-    int t = 0;
-    int64_t chi = 0;
-    std::vector<uint64_t> G, F, M, V, S;
-    std::vector<uint8_t> gam, phase, ck;
-    std::vector<int32_t> cr;
-};
-
 // Device copy of the expansion; allocated once per (device, t) with plain
 // cudaMalloc and kept for the life of the process (never freed, so no CUDA
 // call runs from a static destructor).
@@ -208,78 +200,56 @@ struct TTensorDev {
 };
 
 template <typename T>
-T* dev_copy(const std::vector<T>& h) {
+T* dev_alloc_forever(size_t count, cudaStream_t st) {  // zeroed in stream order
     T* p = nullptr;
-    size_t bytes = std::max<size_t>(h.size(), 1) * sizeof(T);
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
     cudaError_t e = cudaMalloc((void**)&p, bytes);
     if (e == cudaErrorMemoryAllocation) raise(NSG_ERR_OUT_OF_MEMORY, (int64_t)bytes, -1, "device allocation failed");
     cuda_check(e, "cudaMalloc");
-    if (!h.empty()) cuda_check(cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy");
+    cuda_check(cudaMemsetAsync(p, 0, bytes, st), "cudaMemsetAsync");
     return p;
 }
 
 std::mutex g_cache_mu;
-std::map<int, std::shared_ptr<TTensorHost>> g_tt_host;
 std::map<std::pair<int, int>, std::shared_ptr<TTensorDev>> g_tt_dev;
 
-std::shared_ptr<TTensorHost> t_tensor_host(int t) {
-    {
-        std::lock_guard<std::mutex> lk(g_cache_mu);
-        auto it = g_tt_host.find(t);
-        if (it != g_tt_host.end()) return it->second;
+TSmallTerm small_term(const HostCH& c, HScalar coef) {
+    TSmallTerm r;
+    std::memset(&r, 0, sizeof(r));
+    for (int i = 0; i < c.n && i < 6; i++) {
+        r.G[i] = c.G[i].w[0];
+        r.F[i] = c.F[i].w[0];
+        r.M[i] = c.M[i].w[0];
+        r.gam[i] = c.gam[i];
     }
-    auto h = std::make_shared<TTensorHost>();
-    h->t = t;
-    if (t == 0) {  // the Clifford-only circuit: one term |0^n⟩ with coefficient 1
-        h->chi = 1;
-        h->G.assign(1, 0);
-        h->F.assign(1, 0);
-        h->M.assign(1, 0);
-        h->gam.assign(1, 0);
-        h->V.assign(1, 0);
-        h->S.assign(1, 0);
-        h->phase.assign(1, 0);
-        h->ck.assign(1, 0);
-        h->cr.assign(1, 0);
-    } else {
-        HostDecomp d;
-        try {
-            d = t_tensor_state(t);
-        } catch (const HostError& e) {
-            raise(NSG_ERR_DEVICE_INVARIANT, e.code, e.a, "T-state expansion failed (%d)", e.code);
-        }
-        h->chi = (int64_t)d.terms.size();
-        size_t rows = (size_t)h->chi * t;
-        h->G.resize(rows);
-        h->F.resize(rows);
-        h->M.resize(rows);
-        h->gam.resize(rows);
-        h->V.resize(h->chi);
-        h->S.resize(h->chi);
-        h->phase.resize(h->chi);
-        h->ck.resize(h->chi);
-        h->cr.resize(h->chi);
-        for (int64_t i = 0; i < h->chi; i++) {
-            const HostCH& c = d.terms[i];
-            for (int r = 0; r < t; r++) {
-                h->G[i * t + r] = c.G[r].w[0];
-                h->F[i * t + r] = c.F[r].w[0];
-                h->M[i * t + r] = c.M[r].w[0];
-                h->gam[i * t + r] = c.gam[r];
-            }
-            h->V[i] = c.v[0];
-            h->S[i] = c.s[0];
-            h->phase[i] = (uint8_t)c.phase;
-            h->ck[i] = (uint8_t)d.coef[i].k;
-            h->cr[i] = d.coef[i].r;
-        }
-    }
-    std::lock_guard<std::mutex> lk(g_cache_mu);
-    g_tt_host[t] = h;
-    return h;
+    r.v = c.v[0];
+    r.s = c.s[0];
+    r.phase = (uint8_t)c.phase;
+    r.k = coef.k;
+    r.r = coef.r;
+    return r;
 }
 
-std::shared_ptr<TTensorDev> t_tensor_dev(int t, cudaStream_t st) {
+// The cat-state pieces the device expansion of |T⟩^{⊗t} joins (t ≤ 64): the
+// terms of cat(m0) and of cat(6), built on the host (≤ 6 qubits each).
+TPrelude t_prelude(int t) {
+    TPrelude pre;
+    pre.t = t;
+    pre.L = t > 6 ? (t - 3) / 4 : 0;
+    pre.m0 = t - 4 * pre.L;
+    try {
+        HostDecomp base = cat_state(pre.m0), six = cat_state(6);
+        pre.nbase = (int)base.terms.size();
+        for (int i = 0; i < pre.nbase; i++) pre.base[i] = small_term(base.terms[i], base.coef[i]);
+        for (int j = 0; j < 3; j++) pre.cat6[j] = small_term(six.terms[j], six.coef[j]);
+    } catch (const HostError& e) {
+        raise(NSG_ERR_DEVICE_INVARIANT, e.code, e.a, "cat-state construction failed (%d)", e.code);
+    }
+    return pre;
+}
+
+// The expansion of |T⟩^{⊗t} on the device, built once per (device, t).
+std::shared_ptr<TTensorDev> t_tensor_dev(int t, cudaStream_t st, int* status) {
     int dev = 0;
     CK(cudaGetDevice(&dev));
     {
@@ -287,20 +257,58 @@ std::shared_ptr<TTensorDev> t_tensor_dev(int t, cudaStream_t st) {
         auto it = g_tt_dev.find({dev, t});
         if (it != g_tt_dev.end()) return it->second;
     }
-    auto h = t_tensor_host(t);
     auto d = std::make_shared<TTensorDev>();
-    d->chi = h->chi;
     CK(cudaStreamSynchronize(st));
-    d->G = dev_copy(h->G);
-    d->F = dev_copy(h->F);
-    d->M = dev_copy(h->M);
-    d->gam = dev_copy(h->gam);
-    d->V = dev_copy(h->V);
-    d->S = dev_copy(h->S);
-    d->phase = dev_copy(h->phase);
-    d->ck = dev_copy(h->ck);
-    d->cr = dev_copy(h->cr);
+    if (t == 0) {  // the Clifford-only circuit: one empty term, coefficient 1
+        d->chi = 1;
+        d->G = dev_alloc_forever<uint64_t>(1, st);
+        d->F = dev_alloc_forever<uint64_t>(1, st);
+        d->M = dev_alloc_forever<uint64_t>(1, st);
+        d->gam = dev_alloc_forever<uint8_t>(1, st);
+        d->V = dev_alloc_forever<uint64_t>(1, st);
+        d->S = dev_alloc_forever<uint64_t>(1, st);
+        d->phase = dev_alloc_forever<uint8_t>(1, st);
+        d->ck = dev_alloc_forever<uint8_t>(1, st);
+        d->cr = dev_alloc_forever<int32_t>(1, st);
+        CK(cudaStreamSynchronize(st));  // the cache is shared by every stream
+    } else {
+        const TPrelude pre = t_prelude(t);
+        int64_t chi_cat = pre.nbase;
+        for (int l = 0; l < pre.L; l++) chi_cat *= 3;
+        d->chi = 2 * chi_cat;
+        const size_t rows = (size_t)d->chi * t;
+        d->G = dev_alloc_forever<uint64_t>(rows, st);
+        d->F = dev_alloc_forever<uint64_t>(rows, st);
+        d->M = dev_alloc_forever<uint64_t>(rows, st);
+        d->gam = dev_alloc_forever<uint8_t>(rows, st);
+        d->V = dev_alloc_forever<uint64_t>(d->chi, st);
+        d->S = dev_alloc_forever<uint64_t>(d->chi, st);
+        d->phase = dev_alloc_forever<uint8_t>(d->chi, st);
+        d->ck = dev_alloc_forever<uint8_t>(d->chi, st);
+        d->cr = dev_alloc_forever<int32_t>(d->chi, st);
+        TTensorOut o;
+        o.G = d->G;
+        o.F = d->F;
+        o.M = d->M;
+        o.V = d->V;
+        o.S = d->S;
+        o.gam = d->gam;
+        o.phase = d->phase;
+        o.ck = d->ck;
+        o.cr = d->cr;
+        CK(launch_t_tensor(pre, chi_cat, o, status, st));
+        int h = 0;
+        CK(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (h) {
+            CK(cudaMemsetAsync(status, 0, sizeof(int), st));
+            CK(cudaStreamSynchronize(st));
+            raise(NSG_ERR_DEVICE_INVARIANT, h, t, "T-state expansion failed on the device (status %d, t = %d)", h, t);
+        }
+    }
     std::lock_guard<std::mutex> lk(g_cache_mu);
+    auto it = g_tt_dev.find({dev, t});
+    if (it != g_tt_dev.end()) return it->second;  // another thread finished first (its copy is kept)
     g_tt_dev[{dev, t}] = d;
     return d;
 }
@@ -1310,7 +1318,7 @@ nsg_status nsg_state_from_circuit(uint32_t num_qubits, const nsg_gate* gates, si
     auto s = std::make_unique<nsg_state>();
     s->init_stream();
     cudaStream_t st = s->st;
-    auto tt = t_tensor_dev(t, st);
+    auto tt = t_tensor_dev(t, st, s->status.p);
     DBuf<uint32_t> dops;
     dops.alloc(std::max<size_t>(ops.size(), 1), st);
     if (!ops.empty()) CK(cudaMemcpyAsync(dops.p, ops.data(), ops.size() * 4, cudaMemcpyHostToDevice, st));
@@ -1943,6 +1951,50 @@ nsg_status nsg_probe_int_ops(uint64_t iters, double* seconds, uint64_t* ops) {
     cudaStreamDestroy(st);
     *seconds = ms * 1e-3;
     *ops = (uint64_t)blocks * threads * iters * 16 * 8;
+    API_END
+}
+
+nsg_status nsg_debug_t_tensor(uint32_t t, nsg_state** out) {
+    API_BEGIN
+    need(out, "out");
+    *out = nullptr;
+    if (t == 0 || t > 64) raise(NSG_ERR_INVALID_ARGUMENT, t, 64, "t must be in 1..64, got %u", t);
+    auto probe = std::make_unique<nsg_state>();
+    probe->init_stream();
+    auto tt = t_tensor_dev((int)t, probe->st, probe->status.p);
+    const size_t chi = (size_t)tt->chi, rows = chi * t;
+    std::vector<uint64_t> G(rows), F(rows), M(rows), V(chi), S(chi);
+    std::vector<uint8_t> gam(rows), ph(chi), ck(chi);
+    std::vector<int32_t> cr(chi);
+    cudaStream_t st = probe->st;
+    CK(cudaMemcpyAsync(G.data(), tt->G, rows * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(F.data(), tt->F, rows * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(M.data(), tt->M, rows * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(gam.data(), tt->gam, rows, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(V.data(), tt->V, chi * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(S.data(), tt->S, chi * 8, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ph.data(), tt->phase, chi, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(ck.data(), tt->ck, chi, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(cr.data(), tt->cr, chi * 4, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // The term-dump layout of nsg_state_from_terms: bits as bytes, γ as Z8 (2·exponent of i).
+    std::vector<uint8_t> bG(rows * t), bF(rows * t), bM(rows * t), bgam(rows), bv(rows), bs(rows);
+    for (size_t i = 0; i < chi; i++)
+        for (uint32_t r = 0; r < t; r++) {
+            const size_t row = i * t + r;
+            for (uint32_t c = 0; c < t; c++) {
+                bG[row * t + c] = (G[row] >> c) & 1;
+                bF[row * t + c] = (F[row] >> c) & 1;
+                bM[row * t + c] = (M[row] >> c) & 1;
+            }
+            bgam[row] = (uint8_t)(2 * gam[row]);
+            bv[row] = (V[i] >> r) & 1;
+            bs[row] = (S[i] >> r) & 1;
+        }
+    const double gf[2] = {1.0, 0.0};
+    nsg_status rc = nsg_state_from_terms(t, chi, bG.data(), bF.data(), bM.data(), bgam.data(), bv.data(), bs.data(),
+                                         ph.data(), ck.data(), cr.data(), nullptr, gf, out);
+    if (rc != NSG_OK) return rc;
     API_END
 }
 

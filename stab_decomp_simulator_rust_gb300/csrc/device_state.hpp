@@ -71,6 +71,34 @@ enum DevStatus : int {
 
 // ---- launchers (kernels_*.cu) ------------------------------------------------
 
+// |T⟩^{⊗t} expansion on the device.  A small term (width ≤ 6) of the cat
+// states the expansion is assembled from: rows of G, F, M, γ per row, v, s,
+// phase, and its coefficient e^{iπk/4}·2^{-r/2}.
+struct TSmallTerm {
+    uint64_t G[6], F[6], M[6];
+    uint8_t gam[6];
+    uint8_t phase;
+    uint8_t pad;
+    uint64_t v, s;
+    int32_t k, r;
+};
+// cat(t) for t > 6 is cat(m0) joined L times with cat(6) (m0 = t − 4L ∈ [3, 6];
+// for t ≤ 6, m0 = t and L = 0): the host supplies the terms of both.
+struct TPrelude {
+    int t = 0, m0 = 0, L = 0, nbase = 0;
+    TSmallTerm base[3];
+    TSmallTerm cat6[3];
+};
+// The expansion in the layout the compile kernel reads: per term t rows.
+struct TTensorOut {
+    uint64_t *G = nullptr, *F = nullptr, *M = nullptr, *V = nullptr, *S = nullptr;
+    uint8_t *gam = nullptr, *phase = nullptr, *ck = nullptr;
+    int32_t* cr = nullptr;
+};
+// Builds all 2·χ_cat terms of |T⟩^{⊗t} (t ≤ 64); status bit DS_INVARIANT if a
+// projection the construction relies on turns out impossible.
+cudaError_t launch_t_tensor(const TPrelude& pre, int64_t chi_cat, TTensorOut out, int* status, cudaStream_t st);
+
 // Compile: build |0^n⟩⊗T-term, apply the primitive op list, post-select the t
 // ancillas (reverse order) and discard them.  T-terms have width t ≤ 64 in
 // one word per row.  Writes unpacked results to `out` at the term's index and

@@ -208,6 +208,111 @@ __global__ void __launch_bounds__(WARPS * 32) compile_kernel(
     if (ok) store_term<W>(e, out, term);
 }
 
+// ---- |T⟩^{⊗t} expansion --------------------------------------------------------
+// cat_state.rs:162-188 builds cat(m) for m > 6 from cat(m−4) and cat(6): every
+// pair of terms is joined (kron), then Sdg(q0), CX(q0, q1), H(q0) on the two
+// boundary qubits q0 = m−5, q1 = m−4, both projected onto |0⟩ and discarded.
+// Unrolled, term ci of cat(t) is base term i0 of cat(m0) joined with cat(6)
+// terms j_1..j_L, ci = ((i0·3 + j_1)·3 + …)·3 + j_L (the product is i-major,
+// stabilizer_decomposed_state/kron.rs:11-16), and its coefficient is the
+// product of theirs.  t_state.rs:29-71 appends an X·S copy of every term
+// (coefficient × e^{-iπ/4}) and scales all by 2^{-1/2}.  One warp builds one
+// term with the same rules in the same order as the host construction.
+template <int W>
+__device__ __forceinline__ BV<uint64_t, W> small_row(uint64_t x, int off) {
+    BV<uint64_t, W> r = BV<uint64_t, W>::zero();
+    for (int c = 0; c < 6; c++)
+        if ((x >> c) & 1) r.set(off + c, true);
+    return r;
+}
+
+template <int W>
+__device__ __forceinline__ void join_small(Eng<W>& e, const TSmallTerm& b, int off) {
+#pragma unroll
+    for (int k = 0; k < 2 * W; k++) {
+        const int r = 32 * k + e.lane;
+        if (r >= off && r < off + 6) {
+            e.G[k] = small_row<W>(b.G[r - off], off);
+            e.F[k] = small_row<W>(b.F[r - off], off);
+            e.M[k] = small_row<W>(b.M[r - off], off);
+            e.gam_set(k, b.gam[r - off]);
+        }
+    }
+    e.v = e.v | small_row<W>(b.v, off);
+    e.s = e.s | small_row<W>(b.s, off);
+    e.phase = (e.phase + b.phase) & 7;
+}
+
+template <int W>
+__global__ void __launch_bounds__(WARPS * 32) t_tensor_kernel(TPrelude pre, int64_t chi_cat, TTensorOut out,
+                                                              int* __restrict__ status) {
+    const int lane = threadIdx.x & 31;
+    const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    if (term >= 2 * chi_cat) return;  // warp-uniform
+    const bool xs_copy = term >= chi_cat;
+    int64_t ci = xs_copy ? term - chi_cat : term;
+    int dig[16];
+    for (int l = pre.L; l >= 1; l--) {
+        dig[l] = (int)(ci % 3);
+        ci /= 3;
+    }
+    const TSmallTerm& b0 = pre.base[ci];
+    Eng<W> e;
+    e.lane = lane;
+    e.init_zero(0);
+    e.n = 0;
+    join_small<W>(e, b0, 0);
+    e.n = pre.m0;
+    int ck = b0.k, cr = b0.r;
+    bool ok = true;
+    for (int l = 1; l <= pre.L && ok; l++) {
+        const int w = pre.m0 + 4 * (l - 1);
+        const TSmallTerm& b = pre.cat6[dig[l]];
+        join_small<W>(e, b, w);
+        e.n = w + 6;
+        ck += b.k;
+        cr += b.r;
+        const int q0 = w - 1, q1 = w;
+        e.left_sdg(q0);
+        e.left_cx(q0, q1);
+        e.left_h(q0);
+        if (e.project(q0, false) < 0 || e.project(q1, false) < 0) ok = false;
+        if (ok) {
+            e.discard(q1);
+            e.discard(q0);
+        }
+        if (e.err) ok = false;
+    }
+    if (ok && xs_copy) {
+        e.left_x(0);
+        e.left_s(0);
+        ck += 7;
+    }
+    if (!ok || e.err) {
+        if (lane == 0) atomicOr(status, DS_INVARIANT);
+        return;
+    }
+    const int t = pre.t;
+#pragma unroll
+    for (int k = 0; k < 2 * W; k++) {
+        const int r = 32 * k + lane;
+        if (r < t) {
+            const size_t idx = (size_t)term * t + r;
+            out.G[idx] = e.G[k].w[0];
+            out.F[idx] = e.F[k].w[0];
+            out.M[idx] = e.M[k].w[0];
+            out.gam[idx] = (uint8_t)e.gam_of(k);
+        }
+    }
+    if (lane == 0) {
+        out.V[term] = e.v.w[0];
+        out.S[term] = e.s.w[0];
+        out.phase[term] = (uint8_t)e.phase;
+        out.ck[term] = (uint8_t)(ck & 7);
+        out.cr[term] = cr + 1;  // × ONE_OVER_SQRT_2 (t_state.rs:59-64)
+    }
+}
+
 // ---- compaction -------------------------------------------------------------
 __global__ void scan_keep_kernel(const int32_t* __restrict__ keep, int64_t n, int32_t* __restrict__ pos,
                                  int64_t* __restrict__ count) {
@@ -454,6 +559,16 @@ cudaError_t launch_compile(const uint32_t* d_ops, int nops, int n, int t, int64_
     else
         compile_kernel<2><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase, tCk,
                                                   tCr, out, keep, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_t_tensor(const TPrelude& pre, int64_t chi_cat, TTensorOut out, int* status, cudaStream_t st) {
+    if (chi_cat == 0) return cudaSuccess;
+    dim3 grid(blocks_for(2 * chi_cat)), block(WARPS * 32);
+    if (pre.t + 2 <= 64)  // the widest intermediate term has t + 2 qubits
+        t_tensor_kernel<1><<<grid, block, 0, st>>>(pre, chi_cat, out, status);
+    else
+        t_tensor_kernel<2><<<grid, block, 0, st>>>(pre, chi_cat, out, status);
     return cudaGetLastError();
 }
 

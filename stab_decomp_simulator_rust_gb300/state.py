@@ -69,6 +69,13 @@ class QuantumState:
         return QuantumState(h)
 
     @staticmethod
+    def debug_t_tensor(t: int) -> "QuantumState":
+        """The device expansion of |T⟩^{⊗t} as a state (terms in the reference's order)."""
+        h = C.c_void_p()
+        check(_ffi.load().nsg_debug_t_tensor(t, C.byref(h)))
+        return QuantumState(h)
+
+    @staticmethod
     def from_terms(d: dict) -> "QuantumState":
         """Build from a term dump (the layout of ``export_terms``)."""
         L = _ffi.load()

@@ -64,6 +64,15 @@ def test_small_benchmark_circuit_bit_exact(gpu_pkg, oracle):
     assert_same_terms(st.export_terms(), ref.export_terms())
 
 
+@pytest.mark.parametrize("t", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 16, 21, 24])
+def test_device_t_tensor_bit_exact(gpu_pkg, oracle, t):
+    """The device expansion of |T⟩^{⊗t} (t_state.rs:29-71): every term, phase and
+    coefficient in the oracle's order."""
+    dg = gpu_pkg.QuantumState.debug_t_tensor(t).export_terms()
+    dr = oracle.OracleState.t_tensor(t).export_terms()
+    assert_same_terms(dg, dr)
+
+
 @pytest.mark.parametrize("n,nc,nt,seed", [(3, 40, 4, 31), (6, 100, 10, 32), (12, 200, 8, 33),
                                           (33, 300, 7, 34), (40, 400, 9, 35)])
 def test_pair_values_exact(gpu_pkg, oracle, n, nc, nt, seed):
