@@ -8,9 +8,10 @@ terms, and 64 random dense Pauli observables (each qubit uniform in
 (472,878 term pairs per observable).
 
 * ``value``: ⟨P⟩/s with the compiled state resident in HBM; the 64
-  observables go through one batched pass (nsg_exp_value_batch, FP64
-  accumulation), device-timed with CUDA events on the state's stream; L2 is
-  flushed (a 256 MiB write) before every timed step.
+  observables go through one batched pass captured as a plan (nsg_plan_run:
+  one CUDA-graph replay per step, FP64 accumulation), device-timed with CUDA
+  events on torch's stream; L2 is flushed (a 256 MiB write) before every
+  timed step.  ``direct``: the same through nsg_exp_value_batch.
 * ``e2e``: the same metric end to end through the C ABI from host buffers:
   nsg_state_from_circuit (gate list from pinned host memory) +
   nsg_exp_value_batch (Paulis from host, 64 doubles back), wall-clock.
@@ -198,7 +199,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    from stab_decomp_simulator_rust_gb300 import PRECISION_FP64, PRECISION_MIXED, PauliString, QuantumState
+    from stab_decomp_simulator_rust_gb300 import PRECISION_FP64, PRECISION_MIXED, BatchPlan, PauliString, QuantumState
     from stab_decomp_simulator_rust_gb300 import _ffi, build
     build.build()
     L = _ffi.load()
@@ -215,15 +216,16 @@ def run_ours(args):
     chi = st.stabilizer_rank
     pairs = chi * (chi + 1) // 2
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    # The batched evaluation as a captured plan (one CUDA-graph replay per step:
+    # frames, term tables, Pauli frames, pair launch, reduction, result copy).
+    plan = BatchPlan([st], [paulis], PRECISION_FP64)
     for _ in range(args.warmup):
-        st.exp_values(paulis)
+        plan.run()
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
     clocks = ClockSampler(local)
     clocks.start()
-    _ffi.check(L.nsg_profile_enable(1))
-    _ffi.check(L.nsg_profile_read(None, None, None))
     total_ms = 0.0
     results = None
     for _ in range(args.steps):
@@ -231,17 +233,34 @@ def run_ours(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        results = st.exp_values(paulis)
+        results = plan.run()[0]
         e1.record(stream)
         e1.synchronize()
         total_ms += e0.elapsed_time(e1)
     torch.cuda.synchronize()
+    clocks.stop()
+    ms_step, value = combine_ranks(total_ms / args.steps, nobs, "cuda")
+    # the same evaluation through the direct batched call (descriptors built per
+    # call), with the pair kernel's own launches timed on its stream (roofline)
+    for _ in range(2):
+        st.exp_values(paulis)
     import ctypes as C
+    _ffi.check(L.nsg_profile_enable(1))
+    _ffi.check(L.nsg_profile_read(None, None, None))
+    direct_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st.exp_values(paulis)
+        e1.record(stream)
+        e1.synchronize()
+        direct_ms += e0.elapsed_time(e1)
+    direct_ms /= args.steps
     pk_ms, pk_launch, pk_pairs = C.c_double(), C.c_uint64(), C.c_uint64()
     _ffi.check(L.nsg_profile_read(C.byref(pk_ms), C.byref(pk_launch), C.byref(pk_pairs)))
     _ffi.check(L.nsg_profile_enable(0))
-    clocks.stop()
-    ms_step, value = combine_ranks(total_ms / args.steps, nobs, "cuda")
 
     # ---- mixed precision and the single-observable drop-in path
     for _ in range(2):
@@ -303,12 +322,15 @@ def run_ours(args):
                        "chi": chi, "pairs_per_observable": pairs, "observables_per_step": nobs,
                        "l2": "flushed (256 MiB write) before every timed step", "parallelism": f"replicas x{ws}"},
             "inner_products_per_s": value * pairs,
+            "path": "BatchPlan.run (nsg_plan_run: CUDA-graph replay), FP64",
+            "direct": {"value": ws * nobs / (direct_ms * 1e-3), "unit": UNIT, "ms_per_step": direct_ms,
+                       "path": "nsg_exp_value_batch"},
             "mixed": {"value": ws * nobs / (mixed_ms * 1e-3), "unit": UNIT,
                       "max_abs_diff_vs_fp64": float(np.max(np.abs(np.asarray(mixed) - np.asarray(results))))},
             "plain": {"value": plain_rate * ws, "unit": UNIT, "path": "nsg_exp_value, one observable per call"},
             "e2e": e2e, "roofline": roofline, "clocks": clocks.summary(), "gpu_launches": None}
-    # kernels launched per timed step: pauli_frames + pairs + reduce (frames cached)
-    line["gpu_launches"] = 3 * args.steps
+    # kernels launched per timed step (one plan replay): frames, term tables, Pauli frames, pairs, reduction
+    line["gpu_launches"] = 5 * args.steps
     if rank == 0:
         if not args.no_cpu:
             try:

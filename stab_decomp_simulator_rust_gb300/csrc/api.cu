@@ -601,12 +601,85 @@ struct UnitSources {
     const void* ktab = nullptr;
 };
 
+// ---- tuning of captured batches ----------------------------------------------
+// The kernel variant (blocks per SM its registers allow) that ran fastest on a
+// sample, per device and workload class; also appended to the file named by
+// NSG_TUNE_CACHE, one JSON object per line: {"key": "...", "minb": k}.
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tune;
+bool g_tune_loaded = false;
+constexpr int kMinbCandidates[4] = {2, 3, 4, 5};
+
+std::string tune_key(int device, int wb, int nobs_max, int n_mean, uint64_t pairs) {
+    cudaDeviceProp prop;
+    std::string name = "gpu";
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) name = prop.name;
+    for (char& c : name)
+        if (c == '"' || c == '\\' || c == ' ') c = '_';
+    int lg = 0;
+    while ((pairs >> lg) > 1) lg++;
+    char buf[256];
+    std::snprintf(buf, sizeof(buf), "%s|w%d|g%d|n%d|p%d", name.c_str(), wb * 8, (nobs_max + 31) / 32,
+                  (n_mean + 7) / 8 * 8, lg / 2 * 2);
+    return buf;
+}
+
+void tune_load_locked() {
+    if (g_tune_loaded) return;
+    g_tune_loaded = true;
+    const char* path = std::getenv("NSG_TUNE_CACHE");
+    if (!path || !*path) return;
+    FILE* f = std::fopen(path, "r");
+    if (!f) return;
+    char line[512];
+    while (std::fgets(line, sizeof(line), f)) {
+        char key[256];
+        int minb = 0;
+        if (std::sscanf(line, " {\"key\": \"%255[^\"]\", \"minb\": %d}", key, &minb) == 2 && minb >= 2 && minb <= 5)
+            g_tune[key] = minb;
+    }
+    std::fclose(f);
+}
+
+bool tune_lookup(const std::string& key, int& minb) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked();
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) return false;
+    minb = it->second;
+    return true;
+}
+
+void tune_store(const std::string& key, int minb) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked();
+    g_tune[key] = minb;
+    const char* path = std::getenv("NSG_TUNE_CACHE");
+    if (!path || !*path) return;
+    if (FILE* f = std::fopen(path, "a")) {
+        std::fprintf(f, "{\"key\": \"%s\", \"minb\": %d}\n", key.c_str(), minb);
+        std::fclose(f);
+    }
+}
+
+// The pair-kernel variant when nothing was tuned for a workload class, from
+// full-launch timings on GB300 (χ = 972 at n = 28 and 40, χ = 2916 at n = 60;
+// 1, 64 and 256 observables): five blocks per SM for 32-bit rows; for 64-bit
+// rows four up to n = 48, beyond that three, or two with more than 128
+// observables (their per-lane state needs the registers).
+int default_minb(int wb, int nobs_max, int n_mean) {
+    if (wb == 4) return 5;
+    if (n_mean <= 48) return 4;
+    return nobs_max > 128 ? 2 : 3;
+}
+
 // Tiling of a pair launch: kets per chunk, tasks per resident warp, and the
-// kernel variant (blocks per SM its registers allow) for 32- and 64-bit rows.
+// kernel variant (blocks per SM its registers allow) for 32- and 64-bit rows;
+// 0 = the tuning cache's choice for the workload class, else default_minb.
 struct PairTiling {
     int chunk = 32;
     int tasks_per_warp = 4;
-    int minb[2] = {4, 4};
+    int minb[2] = {0, 0};
 };
 
 // Everything one batched evaluation needs on the device, built once
@@ -622,6 +695,7 @@ struct PairBatch {
         std::vector<size_t> units;  // indices into `live`
         size_t out_off = 0;         // first observable of this launch in `dout`
         std::vector<int64_t> task_pairs;  // pairs covered by tasks [0, k) (prefix, for sampled timing)
+        int64_t pairs_total = 0;          // pairs of the whole launch
     };
     std::vector<PairUnit*> live;
     std::vector<UnitSources> src;
@@ -732,7 +806,19 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
                 raise(NSG_ERR_INVALID_ARGUMENT, nobs_max, 32, "complex pair sums take at most 32 observables per launch");
         // Tasks: about tasks_per_warp per resident warp, never spanning two units.
         const size_t warp_smem = pair_warp_smem_bytes(tab_max, bra_max, wb);
-        const int minb = tl.minb[wb == 4 ? 0 : 1];
+        int minb = tl.minb[wb == 4 ? 0 : 1];
+        if (minb == 0) {
+            uint64_t pairs = 0, nsum = 0;
+            for (size_t q = 0; q < sel.size(); q++) {
+                const int64_t chi = b.live[sel[q]]->a->t.chi;
+                pairs += (uint64_t)(chi * (chi + 1) / 2);
+                nsum += (uint64_t)b.live[sel[q]]->a->t.n * (uint64_t)(chi * (chi + 1) / 2);
+            }
+            int dev = 0;
+            CK(cudaGetDevice(&dev));
+            const int n_mean = pairs ? (int)(nsum / pairs) : 0;
+            if (!tune_lookup(tune_key(dev, wb, nobs_max, n_mean, pairs), minb)) minb = default_minb(wb, nobs_max, n_mean);
+        }
         const int64_t resident = pair_resident_warps(wb, nobs_max, warp_smem, minb);
         int64_t total_chunks = 0;
         for (const PairDesc& d : descs) total_chunks += d.nchunks;
@@ -759,6 +845,8 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
                 if (i >= chiA) return chiA * (chiA + 1) / 2;
                 return i * chiA - i * (i - 1) / 2 + std::min<int64_t>((c - off[i]) * tl.chunk, chiA - i);
             };
+            ln.pairs_total = 0;
+            for (size_t q = 0; q < sel.size(); q++) ln.pairs_total += pairs_before(q, descs[q].nchunks);
             const int64_t lim = std::min<int64_t>(total_tasks, 2 * (int64_t)tl.tasks_per_warp * resident);
             ln.task_pairs.assign((size_t)lim + 1, 0);
             int64_t before = 0;  // pairs of the units before q
@@ -1113,73 +1201,13 @@ void sample_marginal(const std::vector<double>& p, const std::vector<std::pair<u
 
 constexpr size_t kMarginalMaxQubits = 8;  // 2^8 Z-strings: one pair pass
 
-// ---- tuning of captured batches ----------------------------------------------
-// The kernel variant (blocks per SM its registers allow) that ran fastest on a
-// sample, per device and workload class; also appended to the file named by
-// NSG_TUNE_CACHE, one JSON object per line: {"key": "...", "minb": k}.
-std::mutex g_tune_mu;
-std::map<std::string, int> g_tune;
-bool g_tune_loaded = false;
-constexpr int kMinbCandidates[4] = {2, 3, 4, 5};
-
-std::string tune_key(int device, int wb, int nobs_max, int n_mean, uint64_t pairs) {
-    cudaDeviceProp prop;
-    std::string name = "gpu";
-    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) name = prop.name;
-    for (char& c : name)
-        if (c == '"' || c == '\\' || c == ' ') c = '_';
-    int lg = 0;
-    while ((pairs >> lg) > 1) lg++;
-    char buf[256];
-    std::snprintf(buf, sizeof(buf), "%s|w%d|g%d|n%d|p%d", name.c_str(), wb * 8, (nobs_max + 31) / 32,
-                  (n_mean + 7) / 8 * 8, lg / 2 * 2);
-    return buf;
-}
-
-void tune_load_locked() {
-    if (g_tune_loaded) return;
-    g_tune_loaded = true;
-    const char* path = std::getenv("NSG_TUNE_CACHE");
-    if (!path || !*path) return;
-    FILE* f = std::fopen(path, "r");
-    if (!f) return;
-    char line[512];
-    while (std::fgets(line, sizeof(line), f)) {
-        char key[256];
-        int minb = 0;
-        if (std::sscanf(line, " {\"key\": \"%255[^\"]\", \"minb\": %d}", key, &minb) == 2 && minb >= 2 && minb <= 5)
-            g_tune[key] = minb;
-    }
-    std::fclose(f);
-}
-
-bool tune_lookup(const std::string& key, int& minb) {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    tune_load_locked();
-    auto it = g_tune.find(key);
-    if (it == g_tune.end()) return false;
-    minb = it->second;
-    return true;
-}
-
-void tune_store(const std::string& key, int minb) {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    tune_load_locked();
-    g_tune[key] = minb;
-    const char* path = std::getenv("NSG_TUNE_CACHE");
-    if (!path || !*path) return;
-    if (FILE* f = std::fopen(path, "a")) {
-        std::fprintf(f, "{\"key\": \"%s\", \"minb\": %d}\n", key.c_str(), minb);
-        std::fclose(f);
-    }
-}
-
-// Device time per pair of one launch of a built batch, on a sample: one task
-// per resident warp (records and counter cleared first).
-double sample_ns_per_pair(PairBatch& b, size_t li, cudaStream_t st) {
+// Device time per pair of one launch of a built batch, on its first tasks
+// (`rounds` per resident warp, or all of them for rounds = 0; records and
+// counter cleared first).  *ms_out receives the launch's time.
+double sample_ns_per_pair(PairBatch& b, size_t li, cudaStream_t st, int rounds, float* ms_out = nullptr) {
     PairBatch::Launch& ln = b.launches[li];
     MultiLaunch m = ln.m;
-    const int64_t k = std::min<int64_t>(m.total_tasks, (int64_t)m.nwarps);
+    const int64_t k = rounds > 0 ? std::min<int64_t>(m.total_tasks, (int64_t)rounds * m.nwarps) : m.total_tasks;
     m.total_tasks = k;
     CK(cudaMemsetAsync(ln.rec.p, 0, ln.rec.n * sizeof(double), st));
     cudaEvent_t e0, e1;
@@ -1193,7 +1221,9 @@ double sample_ns_per_pair(PairBatch& b, size_t li, cudaStream_t st) {
     CK(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    const int64_t pairs = ln.task_pairs.size() > (size_t)k ? ln.task_pairs[(size_t)k] : 0;
+    if (ms_out) *ms_out = ms;
+    const int64_t pairs = k == ln.m.total_tasks ? ln.pairs_total
+                                                 : (ln.task_pairs.size() > (size_t)k ? ln.task_pairs[(size_t)k] : 0);
     return pairs > 0 ? 1e6 * ms / (double)pairs : 1e300;
 }
 
@@ -1630,6 +1660,22 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
         }
         if (need_time[0] || need_time[1]) {
             plan->timed = true;
+            // Whole launches when the default variant's estimate is short, else
+            // two rounds of tasks per resident warp.
+            int rounds[2] = {2, 2};
+            for (size_t k = 0; k < probe.live.size(); k++)
+                CK(launch_pauli_frames(probe.live[k]->a->t.view(), probe.dp.p + probe.unit_obs[k], probe.live[k]->nobs,
+                                       probe.px.p + probe.unit_px[k], probe.pk.p + probe.unit_px[k], st));
+            for (size_t li = 0; li < probe.launches.size(); li++) {
+                const int idx = probe.launches[li].wb == 4 ? 0 : 1;
+                if (!need_time[idx]) continue;
+                float ms = 0.f;
+                sample_ns_per_pair(probe, li, st, 1);
+                sample_ns_per_pair(probe, li, st, 2, &ms);
+                const MultiLaunch& m = probe.launches[li].m;
+                const double frac = (double)std::min<int64_t>(m.total_tasks, 2 * (int64_t)m.nwarps) / (double)m.total_tasks;
+                if (ms / frac < 40.0) rounds[idx] = 0;
+            }
             double best[2] = {1e300, 1e300};
             int pick[2] = {tl.minb[0], tl.minb[1]};
             for (int cand : kMinbCandidates) {
@@ -1644,8 +1690,8 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
                 for (size_t li = 0; li < b.launches.size(); li++) {
                     const int idx = b.launches[li].wb == 4 ? 0 : 1;
                     if (!need_time[idx]) continue;
-                    sample_ns_per_pair(b, li, st);  // first launch of the variant: warm-up
-                    const double ns = sample_ns_per_pair(b, li, st);
+                    sample_ns_per_pair(b, li, st, 1);  // first launch of the variant: warm-up
+                    const double ns = sample_ns_per_pair(b, li, st, rounds[idx]);
                     if (ns < best[idx]) {
                         best[idx] = ns;
                         pick[idx] = cand;

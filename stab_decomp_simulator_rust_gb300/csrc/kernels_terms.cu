@@ -18,6 +18,7 @@ using dev::WarpCH;
 
 constexpr int WARPS = 4;
 constexpr int OPS_CHUNK = 2048;
+constexpr int kCompileWarps = 4;  // warps per block of the compile kernel
 
 template <int W>
 using Eng = WarpCH<uint64_t, W, 2 * W>;
@@ -116,8 +117,10 @@ __device__ __forceinline__ void apply_prim(Eng<W>& e, uint32_t code) {
 }
 
 // ---- compile ------------------------------------------------------------------
-template <int W>
-__global__ void __launch_bounds__(WARPS * 32) compile_kernel(
+// CW warps per block: a compile launch has one warp per T-term, often only a few
+// per SM, so small blocks spread them evenly over the SMs.
+template <int W, int CW>
+__global__ void __launch_bounds__(CW * 32) compile_kernel(
     const uint32_t* __restrict__ ops, int nops, int n, int t, int64_t chi_t,
     const uint64_t* __restrict__ tG, const uint64_t* __restrict__ tF, const uint64_t* __restrict__ tM,
     const uint8_t* __restrict__ tGam, const uint64_t* __restrict__ tV, const uint64_t* __restrict__ tS,
@@ -125,7 +128,7 @@ __global__ void __launch_bounds__(WARPS * 32) compile_kernel(
     TermsView out, int32_t* __restrict__ keep, int* __restrict__ status) {
     __shared__ uint32_t sops[OPS_CHUNK];
     const int lane = threadIdx.x & 31;
-    const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
+    const int64_t term = (int64_t)blockIdx.x * CW + (threadIdx.x >> 5);
     const bool active = term < chi_t;
     const int width = n + t;
 
@@ -552,13 +555,14 @@ cudaError_t launch_compile(const uint32_t* d_ops, int nops, int n, int t, int64_
                            TermsView out, int32_t* keep, int* status, cudaStream_t st) {
     if (chi_t == 0) return cudaSuccess;
     int width = n + t;
-    dim3 grid(blocks_for(chi_t)), block(WARPS * 32);
+    constexpr int CW = kCompileWarps;
+    dim3 grid((unsigned)((chi_t + CW - 1) / CW)), block(CW * 32);
     if (width <= 64)
-        compile_kernel<1><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase, tCk,
-                                                  tCr, out, keep, status);
+        compile_kernel<1, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
+                                                      tCk, tCr, out, keep, status);
     else
-        compile_kernel<2><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase, tCk,
-                                                  tCr, out, keep, status);
+        compile_kernel<2, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
+                                                      tCk, tCr, out, keep, status);
     return cudaGetLastError();
 }
 
