@@ -253,13 +253,11 @@ __global__ void __launch_bounds__(WARPS * 32) t_tensor_kernel(TPrelude pre, int6
     const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (term >= 2 * chi_cat) return;  // warp-uniform
     const bool xs_copy = term >= chi_cat;
-    int64_t ci = xs_copy ? term - chi_cat : term;
-    int dig[16];
-    for (int l = pre.L; l >= 1; l--) {
-        dig[l] = (int)(ci % 3);
-        ci /= 3;
-    }
-    const TSmallTerm& b0 = pre.base[ci];
+    const int64_t ci = xs_copy ? term - chi_cat : term;
+    int64_t p3 = 1;  // 3^L: the digits j_1..j_L are ci mod 3^L, most significant first
+    for (int l = 0; l < pre.L; l++) p3 *= 3;
+    int64_t rem = ci % p3;
+    const TSmallTerm& b0 = pre.base[ci / p3];
     Eng<W> e;
     e.lane = lane;
     e.init_zero(0);
@@ -270,7 +268,9 @@ __global__ void __launch_bounds__(WARPS * 32) t_tensor_kernel(TPrelude pre, int6
     bool ok = true;
     for (int l = 1; l <= pre.L && ok; l++) {
         const int w = pre.m0 + 4 * (l - 1);
-        const TSmallTerm& b = pre.cat6[dig[l]];
+        p3 /= 3;
+        const TSmallTerm& b = pre.cat6[rem / p3];
+        rem %= p3;
         join_small<W>(e, b, w);
         e.n = w + 6;
         ck += b.k;

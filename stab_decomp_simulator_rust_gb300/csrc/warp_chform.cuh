@@ -57,25 +57,25 @@ struct BV {
         for (int k = 0; k < W; k++) r.w[k] = 0;
         return r;
     }
+    // Word selection by a run-time bit index is written with masks over every
+    // word (never a guarded or indexed access), so the vector stays in registers.
     __device__ __forceinline__ bool bit(int q) const {
-        Word x = w[0];
+        Word x = 0;
 #pragma unroll
-        for (int k = 1; k < W; k++)
-            if (q >= k * B) x = w[k];
+        for (int k = 0; k < W; k++) x |= w[k] & ((q / B) == k ? ~(Word)0 : (Word)0);
         return (x >> (q & (B - 1))) & 1;
     }
     __device__ __forceinline__ void flip(int q) {
+        const Word m = (Word)1 << (q & (B - 1));
 #pragma unroll
-        for (int k = 0; k < W; k++)
-            if ((q / B) == k) w[k] ^= (Word)1 << (q & (B - 1));
+        for (int k = 0; k < W; k++) w[k] ^= ((q / B) == k) ? m : (Word)0;
     }
     __device__ __forceinline__ void set(int q, bool b) {
 #pragma unroll
-        for (int k = 0; k < W; k++)
-            if ((q / B) == k) {
-                Word m = (Word)1 << (q & (B - 1));
-                w[k] = b ? (w[k] | m) : (w[k] & ~m);
-            }
+        for (int k = 0; k < W; k++) {
+            const Word m = ((q / B) == k) ? ((Word)1 << (q & (B - 1))) : (Word)0;
+            w[k] = b ? (w[k] | m) : (w[k] & ~m);
+        }
     }
     __device__ __forceinline__ bool any() const {
         Word a = 0;
@@ -211,10 +211,9 @@ struct WarpCH {
         gam = (gam & ~(3u << (2 * sl))) | ((uint32_t)(g & 3) << (2 * sl));
     }
     __device__ __forceinline__ V pick(const V (&X)[RPL], int sl) const {
-        V r = X[0];
+        V r = V::zero();
 #pragma unroll
-        for (int k = 1; k < RPL; k++)
-            if (sl == k) r = X[k];
+        for (int k = 0; k < RPL; k++) r = r | V::select(sl == k, X[k]);
         return r;
     }
     __device__ __forceinline__ V row(const V (&X)[RPL], int q) const {
@@ -224,12 +223,13 @@ struct WarpCH {
         return shfl<uint32_t>((uint32_t)gam_of(q >> 5), q & 31);
     }
     __device__ __forceinline__ bool owns(int q) const { return lane == (q & 31); }
+    // Row updates by a warp-uniform row index are written as masked updates of
+    // every slot (not as a guarded write to slot q >> 5): a guarded write is
+    // turned into an indexed one, which moves the term to local memory.
+    __device__ __forceinline__ bool on_row(int q, int k) const { return owns(q) && (q >> 5) == k; }
     __device__ __forceinline__ void xor_row(V (&X)[RPL], int q, const V& val) {
-        if (owns(q)) {
 #pragma unroll
-            for (int k = 0; k < RPL; k++)
-                if ((q >> 5) == k) X[k] ^= val;
-        }
+        for (int k = 0; k < RPL; k++) X[k] ^= V::select(on_row(q, k), val);
     }
 
     __device__ __forceinline__ void init_zero(int width) {  // StabilizerCHForm::new
@@ -256,15 +256,13 @@ struct WarpCH {
     __device__ __forceinline__ void left_cx(int c, int t) {  // cx.rs:13-51
         V Gc = row(G, c), Ft = row(F, t), Mt = row(M, t);
         int gt = gam_row(t);
-        if (owns(c)) {
 #pragma unroll
-            for (int k = 0; k < RPL; k++)
-                if ((c >> 5) == k) {
-                    int dot = (M[k] & Ft).parity();
-                    gam_set(k, gam_of(k) + gt + 2 * dot);
-                    F[k] ^= Ft;
-                    M[k] ^= Mt;
-                }
+        for (int k = 0; k < RPL; k++) {
+            const bool on = on_row(c, k);
+            const int dot = (M[k] & Ft).parity();
+            gam_set(k, gam_of(k) + (on ? gt + 2 * dot : 0));
+            F[k] ^= V::select(on, Ft);
+            M[k] ^= V::select(on, Mt);
         }
         xor_row(G, t, Gc);
     }
@@ -274,23 +272,18 @@ struct WarpCH {
         xor_row(M, b, Ga);
     }
     __device__ __forceinline__ void left_s_like(int q, int dg) {  // s.rs:13-33 (dg = -1 S, +1 Sdg)
-        if (owns(q)) {
 #pragma unroll
-            for (int k = 0; k < RPL; k++)
-                if ((q >> 5) == k) {
-                    M[k] ^= G[k];
-                    gam_set(k, gam_of(k) + dg);
-                }
+        for (int k = 0; k < RPL; k++) {
+            const bool on = on_row(q, k);
+            M[k] ^= V::select(on, G[k]);
+            gam_set(k, gam_of(k) + (on ? dg : 0));
         }
     }
     __device__ __forceinline__ void left_s(int q) { left_s_like(q, 3); }
     __device__ __forceinline__ void left_sdg(int q) { left_s_like(q, 1); }
     __device__ __forceinline__ void left_z(int q) {  // z.rs:7-14
-        if (owns(q)) {
 #pragma unroll
-            for (int k = 0; k < RPL; k++)
-                if ((q >> 5) == k) gam_set(k, gam_of(k) + 2);
-        }
+        for (int k = 0; k < RPL; k++) gam_set(k, gam_of(k) + (on_row(q, k) ? 2 : 0));
     }
     __device__ __forceinline__ int beta_of(const V& Fq, const V& Mq) const {  // x.rs:20-29
         V b = (Mq & ~v & s) ^ (Fq & v & (Mq ^ s));
