@@ -21,8 +21,9 @@
 // sum of i^{L·z}·(-1)^{zᵀJz} under |¬v_B| linear constraints.  It is reduced
 // variable by variable (constraints by substitution, then each variable
 // summed out: an odd L_j gives √2·ω^{±1} and a rank-one update of J, an even
-// one gives 2·δ(linear form) and a substitution), O(n) steps of O(1) word
-// operations per lane.  The pivots, J and the low bits of L are the same for
+// one gives 2·δ(linear form) and a substitution; variables no longer coupled
+// to any other factor out and are summed out all at once), O(rank J) steps of
+// O(1) word operations per lane.  The pivots, J and the low bits of L are the same for
 // every observable, so one warp reduces one pair for up to 256 observables
 // at once, each lane tracking the per-observable high bits of L, the phase
 // and the constraint right-hand sides of its observables.
@@ -746,8 +747,26 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         if (c[g]) rhs[g] ^= Fk;
                     g_subst<Word, RPL, NG>(kq, lp, c, J, hs, L0, alive, h, ph, own);
                 }
-                // summation, lowest alive variable first
+                // summation: isolated variables (no coupling to another alive one)
+                // factor out and are summed out together; then the lowest alive one
                 while (alive) {
+                    Word iso = 0;
+#pragma unroll
+                    for (int k = 0; k < RPL; k++)
+                        iso |= (Word)__ballot_sync(FULL, (alive & own[k]) && !(J[k] & alive & ~own[k])) << (32 * k);
+                    if (iso) {  // Σ_{z_q} i^{L_q z_q}: 2·δ(hb = 0) for even L_q, √2·ω^{±1} for odd
+                        const Word ie = iso & ~L0, io = iso & L0;
+                        const int nio = popc<Word>(io);
+                        r -= 2 * popc<Word>(ie) + nio;
+#pragma unroll
+                        for (int g = 0; g < NG; g++) {
+                            const Word hbits = hs ^ h[g];
+                            zero[g] |= (hbits & ie) != 0;
+                            ph[g] += nio - 2 * popc<Word>(hbits & io);
+                        }
+                        alive &= ~iso;
+                        if (!alive) break;
+                    }
                     const int jq = ffs0<Word>(alive);
                     const Word jb = (Word)1 << jq;
                     const Word S = row_of<Word, RPL>(J, jq) & alive & ~jb;
