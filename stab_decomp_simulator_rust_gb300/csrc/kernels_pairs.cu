@@ -747,51 +747,48 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         if (c[g]) rhs[g] ^= Fk;
                     g_subst<Word, RPL, NG>(kq, lp, c, J, hs, L0, alive, h, ph, own);
                 }
-                // summation: isolated variables (no coupling to another alive one)
-                // factor out and are summed out together; then the lowest alive one
+                // summation.  A variable removed from `alive` keeps its bits of hs,
+                // h and L0 from then on (every later update is masked by alive),
+                // so the factors that depend only on its own bits are taken at the
+                // end: IE collects summed-out variables with even L (a factor
+                // 2·δ(hb = 0)), IO those with odd L (a factor √2·ω^{1-2hb}).
+                Word IE = 0, IO = 0;
                 while (alive) {
+                    // isolated variables (no coupling to another alive one) factor out
                     Word iso = 0;
 #pragma unroll
                     for (int k = 0; k < RPL; k++)
                         iso |= (Word)__ballot_sync(FULL, (alive & own[k]) && !(J[k] & alive & ~own[k])) << (32 * k);
-                    if (iso) {  // Σ_{z_q} i^{L_q z_q}: 2·δ(hb = 0) for even L_q, √2·ω^{±1} for odd
-                        const Word ie = iso & ~L0, io = iso & L0;
-                        const int nio = popc<Word>(io);
-                        r -= 2 * popc<Word>(ie) + nio;
-#pragma unroll
-                        for (int g = 0; g < NG; g++) {
-                            const Word hbits = hs ^ h[g];
-                            zero[g] |= (hbits & ie) != 0;
-                            ph[g] += nio - 2 * popc<Word>(hbits & io);
-                        }
-                        alive &= ~iso;
-                        if (!alive) break;
-                    }
+                    IE |= iso & ~L0;
+                    IO |= iso & L0;
+                    alive &= ~iso;
+                    if (!alive) break;
+                    // then the lowest alive one, coupled to S
                     const int jq = ffs0<Word>(alive);
                     const Word jb = (Word)1 << jq;
                     const Word S = row_of<Word, RPL>(J, jq) & alive & ~jb;
-                    const bool hsj = (hs >> jq) & 1;
                     alive &= ~jb;
-                    bool hb[NG];
-#pragma unroll
-                    for (int g = 0; g < NG; g++) hb[g] = hsj ^ (bool)((h[g] >> jq) & 1);
                     if ((L0 >> jq) & 1) {  // 1 + i^{L_j}(-1)^{S·z} = √2·ω^{±1}·i^{∓S·z}
-                        r -= 1;
+                        IO |= jb;
 #pragma unroll
-                        for (int g = 0; g < NG; g++) {
-                            ph[g] += hb[g] ? 7 : 1;
-                            if (hb[g]) h[g] ^= S;
-                        }
+                        for (int g = 0; g < NG; g++)
+                            if (((hs ^ h[g]) >> jq) & 1) h[g] ^= S;
                         g_expand<Word, RPL>(J, hs, L0, S, own);
-                    } else {  // 1 + (-1)^{hb + S·z} = 2·δ(S·z = hb)
+                    } else {  // 1 + (-1)^{hb + S·z} = 2·δ(S·z = hb), S ≠ 0 here
                         r -= 2;
-                        if (S == 0) {
+                        bool hb[NG];
+                        const bool hsj = (hs >> jq) & 1;
 #pragma unroll
-                            for (int g = 0; g < NG; g++) zero[g] |= hb[g];
-                        } else {
-                            g_subst<Word, RPL, NG>(ffs0<Word>(S), S & (S - 1), hb, J, hs, L0, alive, h, ph, own);
-                        }
+                        for (int g = 0; g < NG; g++) hb[g] = hsj ^ (bool)((h[g] >> jq) & 1);
+                        g_subst<Word, RPL, NG>(ffs0<Word>(S), S & (S - 1), hb, J, hs, L0, alive, h, ph, own);
                     }
+                }
+                r -= 2 * popc<Word>(IE) + popc<Word>(IO);
+#pragma unroll
+                for (int g = 0; g < NG; g++) {
+                    const Word hbits = hs ^ h[g];
+                    zero[g] |= (hbits & IE) != 0;
+                    ph[g] += popc<Word>(IO) - 2 * popc<Word>(hbits & IO);
                 }
 
                 const int kpair = (kcB - kcA) & 7;
