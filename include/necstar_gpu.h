@@ -216,9 +216,9 @@ nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pauli* pauli,
  * operation that changes a state's rank, width or global factor (projection,
  * discard, measurement) or frees it makes nsg_plan_run fail with
  * NSG_ERR_INVALID_ARGUMENT.  Creation picks the pair-kernel variant for each
- * row width by timing the candidates on a sample of the plan's own work (one
- * task per resident warp), remembered per device and workload class for the
- * process; when the environment variable NSG_TUNE_CACHE names a file, the
+ * row width by timing the candidates on the plan's own work (whole launches
+ * when short, else the first two tasks per resident warp), remembered per
+ * device and workload class for the process; when the environment variable NSG_TUNE_CACHE names a file, the
  * choices are also read from and appended to it (one JSON object per line). */
 typedef struct nsg_plan nsg_plan;
 nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, const nsg_pauli* paulis,
