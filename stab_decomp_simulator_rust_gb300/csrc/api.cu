@@ -610,12 +610,24 @@ std::map<std::string, int> g_tune;
 bool g_tune_loaded = false;
 constexpr int kMinbCandidates[4] = {2, 3, 4, 5};
 
-std::string tune_key(int device, int wb, int nobs_max, int n_mean, uint64_t pairs) {
+// Device names by ordinal (cudaGetDeviceProperties is slow; asked once per device).
+std::string device_name(int device) {
+    static std::mutex mu;
+    static std::map<int, std::string> names;
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = names.find(device);
+    if (it != names.end()) return it->second;
     cudaDeviceProp prop;
     std::string name = "gpu";
     if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) name = prop.name;
     for (char& c : name)
         if (c == '"' || c == '\\' || c == ' ') c = '_';
+    names[device] = name;
+    return name;
+}
+
+std::string tune_key(int device, int wb, int nobs_max, int n_mean, uint64_t pairs) {
+    const std::string name = device_name(device);
     int lg = 0;
     while ((pairs >> lg) > 1) lg++;
     char buf[256];
@@ -709,8 +721,9 @@ struct PairBatch {
     uint64_t pairs = 0;
 };
 
-void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st, uint8_t* dbg_k = nullptr,
-                 int32_t* dbg_r = nullptr) {
+// with_samples: also the pair counts of the first tasks (for timing samples).
+void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st, bool with_samples = false,
+                 uint8_t* dbg_k = nullptr, int32_t* dbg_r = nullptr) {
     const size_t L = b.live.size();
     b.tot_obs = 0;
     size_t tot_px = 0;
@@ -847,7 +860,8 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
             };
             ln.pairs_total = 0;
             for (size_t q = 0; q < sel.size(); q++) ln.pairs_total += pairs_before(q, descs[q].nchunks);
-            const int64_t lim = std::min<int64_t>(total_tasks, 2 * (int64_t)tl.tasks_per_warp * resident);
+            const int64_t lim =
+                with_samples ? std::min<int64_t>(total_tasks, 2 * (int64_t)tl.tasks_per_warp * resident) : 0;
             ln.task_pairs.assign((size_t)lim + 1, 0);
             int64_t before = 0;  // pairs of the units before q
             size_t q = 0;
@@ -994,7 +1008,7 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
     }
     const std::vector<nsg_state*> touched = distinct_states(b.live);
     for (nsg_state* s : touched) join_stream(st, s->st);
-    build_batch(b, PairTiling(), mixed, st, dbg_k, dbg_r);
+    build_batch(b, PairTiling(), mixed, st, false, dbg_k, dbg_r);
     bool prof;
     {
         std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -1281,7 +1295,7 @@ struct nsg_plan {
             if (ps->s == s) return ps.get();
         return nullptr;
     }
-    void build(PairBatch& b, const PairTiling& tl, bool mixed) {
+    void build(PairBatch& b, const PairTiling& tl, bool mixed, bool with_samples = false) {
         b.live = live_units(units);
         b.src.clear();
         for (PairUnit* u : b.live) {
@@ -1291,7 +1305,7 @@ struct nsg_plan {
             src.ktab = find(u->b)->tab.p;
             b.src.push_back(src);
         }
-        build_batch(b, tl, mixed, st);
+        build_batch(b, tl, mixed, st, with_samples);
     }
 };
 
@@ -1642,7 +1656,7 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
     PairTiling tl;
     {
         PairBatch probe;
-        plan->build(probe, tl, mixed);
+        plan->build(probe, tl, mixed, true);
         std::vector<std::string> keys(2);
         bool need_time[2] = {false, false};
         for (const PairBatch::Launch& ln : probe.launches) {
@@ -1683,7 +1697,7 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
                 for (int idx = 0; idx < 2; idx++)
                     if (need_time[idx]) tc.minb[idx] = cand;
                 PairBatch b;
-                plan->build(b, tc, mixed);
+                plan->build(b, tc, mixed, true);
                 for (size_t k = 0; k < b.live.size(); k++)
                     CK(launch_pauli_frames(b.live[k]->a->t.view(), b.dp.p + b.unit_obs[k], b.live[k]->nobs,
                                            b.px.p + b.unit_px[k], b.pk.p + b.unit_px[k], st));

@@ -31,6 +31,9 @@
 
 #include <climits>
 #include <cstdint>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include "device_state.hpp"
 #include "warp_chform.cuh"
@@ -763,8 +766,10 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                     IO |= iso & L0;
                     alive &= ~iso;
                     if (!alive) break;
-                    // then the lowest alive one, coupled to S
-                    const int jq = ffs0<Word>(alive);
+                    // then one coupled variable, with even L if there is one (an even
+                    // step removes two variables, which leaves fewer steps in all)
+                    const Word even = alive & ~L0;
+                    const int jq = ffs0<Word>(even ? even : alive);
                     const Word jb = (Word)1 << jq;
                     const Word S = row_of<Word, RPL>(J, jq) & alive & ~jb;
                     alive &= ~jb;
@@ -1309,9 +1314,23 @@ cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_
 }
 
 int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem, int minb) {
+    // The occupancy query per launch shape, remembered (it costs a driver round trip).
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int, size_t, int>, int> cache;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(dev, word_bytes, (nobs_max + 31) / 32, warp_smem, minb);
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
     const int nb = word_bytes == 4 ? resident_blocks_w<uint32_t, 1>(nobs_max, warp_smem, minb)
                                    : resident_blocks_w<uint64_t, 2>(nobs_max, warp_smem, minb);
-    return nb * PWARPS * device_sm_count();
+    const int w = nb * PWARPS * device_sm_count();
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = w;
+    return w;
 }
 
 cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, int64_t total_obs, double* out,
