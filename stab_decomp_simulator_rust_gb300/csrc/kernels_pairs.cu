@@ -480,6 +480,11 @@ __device__ __forceinline__ void g_subst(int kq, Word lp, const bool (&c)[NG], Wo
 template <typename Word, int RPL, int NG, int MINB>
 __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) {
     constexpr int GMAX = (8 * sizeof(Word)) / 4;  // groups of four rows (8 or 16)
+    // Unrolling of the table-lookup loops: full for 32-bit rows; for 64-bit
+    // rows partial, less with more observables per lane (code size and
+    // registers; from launch timings at n = 40 and 60).
+    constexpr int UNROLL_COMP = sizeof(Word) == 4 ? GMAX : (NG <= 2 ? 4 : 2);
+    constexpr int UNROLL_BRA = sizeof(Word) == 4 ? GMAX : (NG <= 2 ? GMAX : 2);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int gwarp = blockIdx.x * PWARPS + wid;
@@ -643,7 +648,7 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                     fD[k] = yP[k] = Kr[k] = 0;
                     Y[k] = MV[k];
                 }
-#pragma unroll
+#pragma unroll (UNROLL_COMP)
                 for (int g = 0; g < GMAX; g++) {
                     if (g < ngrp) {
                         const Word* TF = T + g * 16;
@@ -658,7 +663,7 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         }
                     }
                 }
-#pragma unroll
+#pragma unroll (UNROLL_BRA)
                 for (int g = 0; g < GMAX; g++) {
                     if (g < ngrp) {
 #pragma unroll
