@@ -438,7 +438,7 @@ struct nsg_state {
     bool frames_ok = false;
     DBuf<uint64_t> fGV, fFV, fMV, fGVL, fGVH;
     DBuf<int> status;
-    // cached ket tables (Four-Russians tables of every term, n ≤ 64)
+    // cached term tables (Four-Russians tables of every term, n ≤ 64)
     bool ket_ok = false;
     DBuf<unsigned char> ktab;
 

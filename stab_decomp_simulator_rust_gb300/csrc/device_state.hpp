@@ -139,6 +139,7 @@ cudaError_t launch_frames(const TermsView& t, FrameView fr, cudaStream_t st);
 cudaError_t launch_pauli_frames(const TermsView& t, const DevPauli* d_paulis, int nobs,
                                 uint64_t* x_out, uint8_t* k_out, cudaStream_t st);
 
+// One launch of the row-staged pair kernel (launch_pairs_rows).
 struct PairLaunch {
     TermsView A;   // bra terms (frames computed from these)
     FrameView fr;  // frames of A
@@ -157,16 +158,12 @@ struct PairLaunch {
     int blocks = 0;
     int warps_per_block = 4;
     int* status = nullptr;
-    const void* ktab = nullptr;  // ket tables of B ([chiB] x ket_table_stride bytes)
-    size_t ktab_stride = 0;
-    int ngrp = 0;
-    size_t warp_smem = 0;        // dynamic shared memory per warp (pair_warp_smem)
-    uint8_t* dbg_k = nullptr;   // optional per-pair dump [chiA][chiB]
+    uint8_t* dbg_k = nullptr;  // optional per-pair dump [chiA][chiB]
     int32_t* dbg_r = nullptr;
 };
 
 // One unit of a batched pair-sum launch: bra terms A (with their frames and
-// Pauli frames) against ket terms B (with their ket tables).
+// Pauli frames) against ket terms B (with their term tables).
 struct PairDesc {
     TermsView A;
     TermsView B;
@@ -216,7 +213,7 @@ struct MultiLaunch {
 };
 
 // word_bytes: 4 when every unit of the launch has n ≤ 32, 8 when every unit
-// has 32 < n ≤ 64 (units are split by word width; ket tables are built with
+// has 32 < n ≤ 64 (units are split by word width; term tables are built with
 // the word width of their state, ket_table_stride).
 cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_t st);
 // out: 2 doubles (re, im) per observable, observables of unit u starting at obs_begin[u].
@@ -226,7 +223,7 @@ size_t pair_warp_smem_bytes(size_t ket_bytes_max, size_t bra_bytes_max, int word
 // Warps of the pair kernel resident on the whole device at once.
 int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem, int minb);
 
-// The same sums with B's rows staged per pair instead of ket tables (no
+// The same sums with B's rows staged per pair instead of term tables (no
 // per-term table storage; at most 32 observables).
 cudaError_t launch_pairs_rows(const PairLaunch& p, cudaStream_t st);
 

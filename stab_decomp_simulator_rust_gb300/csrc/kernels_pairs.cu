@@ -263,7 +263,7 @@ struct ChunkAcc {
     }
 };
 
-// ---- ket tables -----------------------------------------------------------------
+// ---- term tables ----------------------------------------------------------------
 // Per term B, Four-Russians tables (the 16 XOR combinations of each group of
 // four rows) of three matrices the pair kernel multiplies by:
 //   F        the tableau's F rows,
@@ -894,7 +894,7 @@ __global__ void reduce_multi_kernel(MultiLaunch p, const int64_t* __restrict__ o
     }
 }
 
-// Row-staged variant of the pair kernel (no ket tables): B's rows are
+// Row-staged variant of the pair kernel (no term tables): B's rows are
 // staged in shared memory and composed bit by bit.  It needs no per-term
 // table storage, which is what nsg_exp_value_noalloc's fixed scratch
 // affords; one observable per lane group.

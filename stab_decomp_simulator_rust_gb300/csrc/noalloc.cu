@@ -7,7 +7,7 @@
 // cudaMalloc/cudaFree would synchronise the device.  This entry point runs
 // the kernels of nsg_exp_value (bra frames, Pauli frames, the pair sum, the
 // FP64 reduction; the pair sum in its row-staged form, which needs no
-// per-term ket tables) but takes all of their scratch from one file-scope
+// per-term tables) but takes all of their scratch from one file-scope
 // device array, g_noalloc_scratch, of 16 MiB.  Every GPU that loads the
 // library holds that array until the process exits.
 //
