@@ -534,6 +534,25 @@ namespace {
     }                                         \
     return NSG_OK;
 
+// Makes a state's device current for the length of a call (and restores the
+// caller's): a state's memory and stream belong to the device that was current
+// when it was created.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        int cur = 0;
+        if (cudaGetDevice(&cur) == cudaSuccess && cur != dev) {
+            prev = cur;
+            cudaSetDevice(dev);
+        }
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope&) = delete;
+    DeviceScope& operator=(const DeviceScope&) = delete;
+};
+
 void need(const void* p, const char* what) {
     if (!p) raise(NSG_ERR_INVALID_ARGUMENT, -1, -1, "null %s", what);
 }
@@ -1429,12 +1448,17 @@ nsg_status nsg_state_from_terms(uint32_t num_qubits, uint64_t num_terms, const u
     API_END
 }
 
-void nsg_state_free(nsg_state* state) { delete state; }
+void nsg_state_free(nsg_state* state) {
+    if (!state) return;
+    DeviceScope ds_(state->device);
+    delete state;
+}
 
 nsg_status nsg_state_clone(const nsg_state* state, nsg_state** out) {
     API_BEGIN
     need(state, "state");
     need(out, "out");
+    DeviceScope ds_(state->device);
     *out = clone_state(state);
     API_END
 }
@@ -1475,6 +1499,7 @@ nsg_status nsg_state_set_stream(nsg_state* state, void* cuda_stream) {
 nsg_status nsg_apply_gates(nsg_state* state, const nsg_gate* gates, size_t num_gates) {
     API_BEGIN
     need(state, "state");
+    DeviceScope ds_(state->device);
     if (num_gates) need(gates, "gates");
     // apply_gates (stabilizer_decomposed_state/gates.rs:7-37): gates apply in
     // order; the first failing gate stops after its predecessors took effect.
@@ -1524,6 +1549,7 @@ nsg_status nsg_exp_value_batch(const nsg_state* cstate, const nsg_pauli* paulis,
                                uint32_t precision, double* out) {
     API_BEGIN
     need(cstate, "state");
+    DeviceScope ds_(cstate->device);
     if (num_paulis) {
         need(paulis, "paulis");
         need(out, "out");
@@ -1580,7 +1606,7 @@ nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states
         }
     }
     if (!units.empty()) {
-        CK(cudaSetDevice(states[0]->device));
+        DeviceScope ds_(states[0]->device);
         run_pair_units(units, precision == NSG_PRECISION_MIXED, const_cast<nsg_state*>(states[0])->st);
     }
     API_END
@@ -1608,7 +1634,7 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
     const bool mixed = precision == NSG_PRECISION_MIXED;
     auto plan = std::make_unique<nsg_plan>();
     plan->device = num_states ? states[0]->device : 0;
-    CK(cudaSetDevice(plan->device));
+    DeviceScope ds_(plan->device);
     CK(cudaStreamCreateWithFlags(&plan->st, cudaStreamNonBlocking));
     cudaStream_t st = plan->st;
     plan->paulis.resize(total);
@@ -1753,7 +1779,7 @@ nsg_status nsg_plan_run(nsg_plan* plan, double* out) {
     }
     if (!plan->results.empty()) need(out, "out");
     if (plan->exec) {
-        CK(cudaSetDevice(plan->device));
+        DeviceScope ds_(plan->device);
         for (auto& ps : plan->states) join_stream(plan->st, ps->s->st);
         CK(cudaGraphLaunch(plan->exec, plan->st));
         CK(cudaStreamSynchronize(plan->st));
@@ -1785,6 +1811,9 @@ nsg_status nsg_inner_product(const nsg_state* a, const nsg_state* b, double out[
     need(a, "a");
     need(b, "b");
     need(out, "out");
+    if (a->device != b->device)
+        raise(NSG_ERR_INVALID_ARGUMENT, a->device, b->device, "the two states live on different devices");
+    DeviceScope ds_(a->device);
     if (a->t.n != b->t.n)
         raise(NSG_ERR_QUBIT_COUNT_MISMATCH, a->t.n, b->t.n,
               "The qubit counts of the two states must match for calculating inner product, got %d and %d.", a->t.n,
@@ -1804,6 +1833,7 @@ nsg_status nsg_inner_product(const nsg_state* a, const nsg_state* b, double out[
 nsg_status nsg_norm(const nsg_state* state, double* out) {
     API_BEGIN
     need(state, "state");
+    DeviceScope ds_(state->device);
     need(out, "out");
     *out = std::sqrt(norm_squared(const_cast<nsg_state*>(state)));
     API_END
@@ -1812,6 +1842,7 @@ nsg_status nsg_norm(const nsg_state* state, double* out) {
 nsg_status nsg_project_unnormalized(nsg_state* state, uint32_t qubit, int32_t outcome) {
     API_BEGIN
     need(state, "state");
+    DeviceScope ds_(state->device);
     project_unnorm(state, qubit, outcome != 0);
     API_END
 }
@@ -1819,6 +1850,7 @@ nsg_status nsg_project_unnormalized(nsg_state* state, uint32_t qubit, int32_t ou
 nsg_status nsg_project_normalized(nsg_state* state, uint32_t qubit, int32_t outcome) {
     API_BEGIN
     need(state, "state");
+    DeviceScope ds_(state->device);
     project_unnorm(state, qubit, outcome != 0);  // projection.rs:10-21
     double nrm = std::sqrt(norm_squared(state));
     if (std::fabs(nrm) < 1e-12 || std::isnan(nrm)) err_impossible(qubit, outcome != 0);
@@ -1830,6 +1862,7 @@ nsg_status nsg_project_normalized(nsg_state* state, uint32_t qubit, int32_t outc
 nsg_status nsg_discard(nsg_state* state, uint32_t qubit) {
     API_BEGIN
     need(state, "state");
+    DeviceScope ds_(state->device);
     discard_q(state, qubit);
     API_END
 }
@@ -1838,6 +1871,7 @@ nsg_status nsg_measure(nsg_state* state, const uint32_t* qargs, size_t num_qargs
                        uint8_t* out) {
     API_BEGIN
     need(state, "state");
+    DeviceScope ds_(state->device);
     if (num_qargs) {
         need(qargs, "qargs");
         need(out, "out");
@@ -1881,6 +1915,7 @@ nsg_status nsg_sample(const nsg_state* cstate, const uint32_t* qargs, size_t num
                       size_t* num_out) {
     API_BEGIN
     need(cstate, "state");
+    DeviceScope ds_(cstate->device);
     need(num_out, "num_out");
     nsg_state* state = const_cast<nsg_state*>(cstate);
     if (num_qargs) need(qargs, "qargs");
@@ -1914,6 +1949,7 @@ nsg_status nsg_sample(const nsg_state* cstate, const uint32_t* qargs, size_t num
 nsg_status nsg_to_statevector(const nsg_state* state, double* out, size_t capacity_complex) {
     API_BEGIN
     need(state, "state");
+    DeviceScope ds_(state->device);
     const int n = state->t.n;
     if (n > 28)
         raise(NSG_ERR_STATEVECTOR_TOO_LARGE, n, -1,
@@ -1937,6 +1973,7 @@ nsg_status nsg_export_terms(const nsg_state* state, uint8_t* G, uint8_t* F, uint
                             double global_factor[2]) {
     API_BEGIN
     need(state, "state");
+    DeviceScope ds_(state->device);
     cudaStream_t st = state->st;
     const int64_t chi = state->t.chi;
     const int n = state->t.n;
@@ -2061,6 +2098,7 @@ nsg_status nsg_debug_t_tensor(uint32_t t, nsg_state** out) {
 nsg_status nsg_debug_pair_values(const nsg_state* cstate, const nsg_pauli* pauli, uint8_t* k, int32_t* r) {
     API_BEGIN
     need(cstate, "state");
+    DeviceScope ds_(cstate->device);
     need(k, "k");
     need(r, "r");
     nsg_state* state = const_cast<nsg_state*>(cstate);
