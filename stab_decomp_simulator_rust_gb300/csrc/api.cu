@@ -709,7 +709,7 @@ int default_minb(int wb, int nobs_max, int n_mean) {
 // 0 = the tuning cache's choice for the workload class, else default_minb.
 struct PairTiling {
     int chunk = 32;
-    int tasks_per_warp = 4;
+    int tasks_per_warp = 8;  // 2, 4, 8 measured on n = 28, 40, 60: 8 fastest (balance at the end of the queue)
     int minb[2] = {0, 0};
 };
 
