@@ -41,8 +41,8 @@ import numpy as np  # noqa: E402
 
 # DRAM bytes (read + write) of one pair-kernel launch of this workload, from one
 # ncu capture (dram__bytes_read.sum + dram__bytes_write.sum): the 5 MB of term
-# tables stay L2-resident, so the kernel does not stream HBM.
-PAIR_TRAFFIC_BYTES = 37_917_184 + 12_032
+# tables stay L2-resident; most of it is the per-task records.
+PAIR_TRAFFIC_BYTES = 69_151_232 + 5_759_488
 
 METRIC = "Pauli \u27e8P\u27e9/s and CH inner products/s, mixed+batched vs plain FP64 @\u22641e-9 err"
 UNIT = "<P>/s"
