@@ -727,6 +727,8 @@ struct PairBatch {
         size_t out_off = 0;         // first observable of this launch in `dout`
         std::vector<int64_t> task_pairs;  // pairs covered by tasks [0, k) (prefix, for sampled timing)
         int64_t pairs_total = 0;          // pairs of the whole launch
+        size_t rec_used = 0;              // doubles of `rec` to clear before a launch (records, counter)
+        double* red_scratch = nullptr;    // partials of the two-pass reduction
     };
     std::vector<PairUnit*> live;
     std::vector<UnitSources> src;
@@ -932,9 +934,13 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
             m.dbg_k = dbg_k;
             m.dbg_r = dbg_r;
         }
-        ln.rec.alloc((size_t)rec_doubles + 1, st);  // records, then the task counter
+        // records, then the task counter, then the reduction's partials
+        const size_t red = (size_t)reduce_splits(ln.obegin.back()) * (size_t)ln.obegin.back() * 8;
+        ln.rec.alloc((size_t)rec_doubles + 1 + red, st);
+        ln.rec_used = (size_t)rec_doubles + 1;
         m.records = ln.rec.p;
         m.counter = (unsigned long long*)(ln.rec.p + rec_doubles);
+        ln.red_scratch = ln.rec.p + rec_doubles + 1;
     }
 }
 
@@ -946,7 +952,7 @@ void enqueue_batch(PairBatch& b, cudaStream_t st, float* pair_ms = nullptr, int6
         CK(launch_pauli_frames(b.live[k]->a->t.view(), b.dp.p + b.unit_obs[k], b.live[k]->nobs,
                                b.px.p + b.unit_px[k], b.pk.p + b.unit_px[k], st));
     for (PairBatch::Launch& ln : b.launches) {
-        CK(cudaMemsetAsync(ln.rec.p, 0, ln.rec.n * sizeof(double), st));
+        CK(cudaMemsetAsync(ln.rec.p, 0, ln.rec_used * sizeof(double), st));
         MultiLaunch m = ln.m;
         if (max_tasks > 0 && max_tasks < m.total_tasks) {
             m.total_tasks = max_tasks;
@@ -970,7 +976,7 @@ void enqueue_batch(PairBatch& b, cudaStream_t st, float* pair_ms = nullptr, int6
             cudaEventDestroy(ev1);
             *pair_ms += ms;
         }
-        CK(launch_reduce_multi(m, ln.d_obegin, ln.obegin.back(), b.dout.p + 2 * ln.out_off, st));
+        CK(launch_reduce_multi(m, ln.d_obegin, ln.obegin.back(), b.dout.p + 2 * ln.out_off, ln.red_scratch, st));
     }
 }
 
@@ -1242,7 +1248,7 @@ double sample_ns_per_pair(PairBatch& b, size_t li, cudaStream_t st, int rounds, 
     MultiLaunch m = ln.m;
     const int64_t k = rounds > 0 ? std::min<int64_t>(m.total_tasks, (int64_t)rounds * m.nwarps) : m.total_tasks;
     m.total_tasks = k;
-    CK(cudaMemsetAsync(ln.rec.p, 0, ln.rec.n * sizeof(double), st));
+    CK(cudaMemsetAsync(ln.rec.p, 0, ln.rec_used * sizeof(double), st));
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));

@@ -217,8 +217,10 @@ struct MultiLaunch {
 // the word width of their state, ket_table_stride).
 cudaError_t launch_pairs_multi(const MultiLaunch& m, int word_bytes, cudaStream_t st);
 // out: 2 doubles (re, im) per observable, observables of unit u starting at obs_begin[u].
+// scratch: reduce_splits(total_obs) · total_obs · 8 doubles.
 cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, int64_t total_obs, double* out,
-                                cudaStream_t st);
+                                double* scratch, cudaStream_t st);
+int reduce_splits(int64_t total_obs);
 size_t pair_warp_smem_bytes(size_t ket_bytes_max, size_t bra_bytes_max, int word_bytes);
 // Warps of the pair kernel resident on the whole device at once.
 int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem, int minb);

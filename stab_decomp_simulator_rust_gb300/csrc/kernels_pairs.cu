@@ -29,6 +29,7 @@
 // and the constraint right-hand sides of its observables.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <climits>
 #include <cstdint>
 #include <map>
@@ -842,34 +843,22 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
     }
 }
 
-// Reduction of the per-task records: one block per (descriptor,
-// observable) over the descriptor's tasks, in a fixed double-double tree.
-__global__ void reduce_multi_kernel(MultiLaunch p, const int64_t* __restrict__ obs_begin, double* __restrict__ out) {
-    __shared__ double sh[8][256];
-    int lo = 0, hi = p.num_descs;  // descriptor of this block's observable
-    const int64_t ob = blockIdx.x;
+// Reduction of the per-task records in two fixed-order passes (deterministic):
+// block (observable, split) folds its slice of the unit's task records into a
+// double-double partial, then one block per observable folds the partials in
+// split order and applies the unit's scale.
+__device__ __forceinline__ int unit_of(const int64_t* __restrict__ begin, int num, int64_t x) {
+    int lo = 0, hi = num;
     while (hi - lo > 1) {
         const int mid = (lo + hi) >> 1;
-        if (obs_begin[mid] <= ob) lo = mid;
+        if (begin[mid] <= x) lo = mid;
         else hi = mid;
     }
-    const int ds = lo;
-    const PairDesc* d = p.descs + ds;
-    const int o = (int)(ob - obs_begin[ds]);
-    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const int64_t ntasks = p.task_begin[ds + 1] - p.task_begin[ds];
-    {
-        for (int64_t tl = threadIdx.x; tl < ntasks; tl += blockDim.x) {
-            const double* pp = p.records + d->rec0 + (tl * d->nobs + o) * 8;
-#pragma unroll
-            for (int t = 0; t < 4; t++) {
-                double s, e;
-                two_sum_d(acc[2 * t], pp[2 * t], s, e);
-                acc[2 * t] = s;
-                acc[2 * t + 1] += e + pp[2 * t + 1];
-            }
-        }
-    }
+    return lo;
+}
+
+// Double-double tree over the block's 256 threads (8 lanes: 4 classes × (hi, lo)).
+__device__ __forceinline__ void block_fold(double (&acc)[8], double (&sh)[8][256]) {
 #pragma unroll
     for (int t = 0; t < 8; t++) sh[t][threadIdx.x] = acc[t];
     __syncthreads();
@@ -885,13 +874,49 @@ __global__ void reduce_multi_kernel(MultiLaunch p, const int64_t* __restrict__ o
         }
         __syncthreads();
     }
-    if (threadIdx.x == 0) {
-        const double r2 = 0.70710678118654752440;
-        const double re = (sh[0][0] + sh[1][0]) + (sh[2][0] + sh[3][0]) * r2;
-        const double im = (sh[4][0] + sh[5][0]) + (sh[6][0] + sh[7][0]) * r2;
-        out[2 * ob] = re * d->scale_re - im * d->scale_im;
-        out[2 * ob + 1] = re * d->scale_im + im * d->scale_re;
+}
+
+__device__ __forceinline__ void dd_add8(double (&acc)[8], const double* __restrict__ pp) {
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+        double s, e;
+        two_sum_d(acc[2 * t], pp[2 * t], s, e);
+        acc[2 * t] = s;
+        acc[2 * t + 1] += e + pp[2 * t + 1];
     }
+}
+
+__global__ void __launch_bounds__(256) reduce_tasks_kernel(MultiLaunch p, const int64_t* __restrict__ obs_begin,
+                                                           int nsplit, double* __restrict__ part) {
+    __shared__ double sh[8][256];
+    const int64_t ob = blockIdx.x;
+    const int split = blockIdx.y;
+    const int ds = unit_of(obs_begin, p.num_descs, ob);
+    const PairDesc* d = p.descs + ds;
+    const int o = (int)(ob - obs_begin[ds]);
+    const int64_t ntasks = p.task_begin[ds + 1] - p.task_begin[ds];
+    const int64_t per = (ntasks + nsplit - 1) / nsplit;
+    const int64_t t0 = (int64_t)split * per, t1 = min(t0 + per, ntasks);
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int64_t tl = t0 + threadIdx.x; tl < t1; tl += blockDim.x)
+        dd_add8(acc, p.records + d->rec0 + (tl * d->nobs + o) * 8);
+    block_fold(acc, sh);
+    if (threadIdx.x < 8) part[((size_t)ob * nsplit + split) * 8 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(32) reduce_final_kernel(MultiLaunch p, const int64_t* __restrict__ obs_begin,
+                                                          int nsplit, const double* __restrict__ part,
+                                                          double* __restrict__ out) {
+    const int64_t ob = (int64_t)blockIdx.x * 32 + threadIdx.x;
+    if (ob >= obs_begin[p.num_descs]) return;
+    const PairDesc* d = p.descs + unit_of(obs_begin, p.num_descs, ob);
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int sp = 0; sp < nsplit; sp++) dd_add8(acc, part + ((size_t)ob * nsplit + sp) * 8);
+    const double r2 = 0.70710678118654752440;
+    const double re = (acc[0] + acc[1]) + (acc[2] + acc[3]) * r2;
+    const double im = (acc[4] + acc[5]) + (acc[6] + acc[7]) * r2;
+    out[2 * ob] = re * d->scale_re - im * d->scale_im;
+    out[2 * ob + 1] = re * d->scale_im + im * d->scale_re;
 }
 
 // Row-staged variant of the pair kernel (no term tables): B's rows are
@@ -1338,10 +1363,20 @@ int pair_resident_warps(int word_bytes, int nobs_max, size_t warp_smem, int minb
     return w;
 }
 
+int reduce_splits(int64_t total_obs) {
+    const int64_t want = 2 * (int64_t)device_sm_count();  // blocks to keep every SM busy
+    const int64_t s = (want + total_obs - 1) / std::max<int64_t>(total_obs, 1);
+    return (int)std::min<int64_t>(std::max<int64_t>(s, 1), 32);
+}
+
 cudaError_t launch_reduce_multi(const MultiLaunch& m, const int64_t* obs_begin, int64_t total_obs, double* out,
-                                cudaStream_t st) {
+                                double* scratch, cudaStream_t st) {
     if (total_obs == 0) return cudaSuccess;
-    reduce_multi_kernel<<<(unsigned)total_obs, 256, 0, st>>>(m, obs_begin, out);
+    const int nsplit = reduce_splits(total_obs);
+    reduce_tasks_kernel<<<dim3((unsigned)total_obs, (unsigned)nsplit), 256, 0, st>>>(m, obs_begin, nsplit, scratch);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    reduce_final_kernel<<<(unsigned)((total_obs + 31) / 32), 32, 0, st>>>(m, obs_begin, nsplit, scratch, out);
     return cudaGetLastError();
 }
 
