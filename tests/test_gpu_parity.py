@@ -292,3 +292,26 @@ def test_error_codes(gpu_pkg):
     with pytest.raises(NecstarError) as e:
         st.exp_value(PS.from_str("ZZZZ"))
     assert e.value.code == 11 and e.value.args3[:2] == (3, 4)
+
+
+@pytest.mark.parametrize("n,nc,nt,seed", [(1, 0, 0, 401), (1, 6, 3, 402), (2, 10, 0, 403), (2, 12, 4, 404),
+                                          (3, 20, 7, 405)])
+def test_tiny_states_every_pauli(gpu_pkg, oracle, n, nc, nt, seed):
+    """Widths 1-3, with and without T gates (χ = 1 included): every dense Pauli,
+    the norm, ⟨0ⁿ|ψ⟩ and the statevector against the oracle."""
+    import itertools
+    gates = random_full_circuit(n, nc, nt, seed) if nc + nt else np.zeros((0, 4), np.uint32)
+    st = gpu_pkg.QuantumState.from_gates(n, gates)
+    ref = oracle.OracleState.from_circuit(n, gates)
+    ops_all = [np.asarray(o, np.uint8) for o in itertools.product(range(4), repeat=n)]
+    got = st.exp_values([gpu_pkg.PauliString.dense(o) for o in ops_all])
+    for o, g in zip(ops_all, got):
+        _, ex = ref.exp_value(0, o)
+        assert close(g, ex), (o, g, ex)
+    assert close(st.norm(), ref.norm()[1] ** 0.5)
+    z = gpu_pkg.QuantumState.from_gates(n, np.zeros((0, 4), np.uint32))
+    rz = oracle.OracleState.from_circuit(n, np.zeros((0, 4), np.uint32))
+    amp = z.inner_product(st)
+    _, amp_ex = rz.inner_product(ref)
+    assert abs(amp - amp_ex) <= TOL
+    assert np.allclose(st.to_statevector(), ref.to_statevector(), atol=1e-12)
