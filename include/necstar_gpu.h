@@ -53,6 +53,8 @@ typedef int32_t nsg_status;
 #define NSG_ERR_NOT_IMPLEMENTED               16
 #define NSG_ERR_PAULI_STRING_PARSING          17
 #define NSG_ERR_INVALID_ARGUMENT              18  /* null pointer, bad enum value */
+#define NSG_ERR_QASM_PARSING                  19  /* QasmParsingError (host-side circuit parser) */
+#define NSG_ERR_IO                            20  /* Io (host-side QASM file writer)             */
 #define NSG_ERR_CUDA                         100  /* args: cudaError_t            */
 #define NSG_ERR_DEVICE_INVARIANT             101  /* args: invariant id, term     */
 #define NSG_ERR_TIMEOUT                      102
@@ -280,6 +282,27 @@ nsg_status nsg_sample(const nsg_state* state, const uint32_t* qargs, size_t num_
  * values as interleaved (re, im); n ≤ 28. */
 nsg_status nsg_to_statevector(const nsg_state* state, double* out, size_t capacity_complex);
 
+/* QuantumCircuit::random_clifford (crates/necstar/src/circuit/mod.rs:289-291
+ * → crates/stabilizer-ch-form-rust/src/circuit/random_clifford.rs:177-212):
+ * a uniformly random n-qubit Clifford as a gate list (Bravyi–Maslov canonical
+ * form U = F1·H·S·F2, drawn and emitted in the reference's order from the
+ * seeded stream below).  out must hold 2n² + 3n gates (the bound; fewer are
+ * written, *num_out of them); seed32 may be NULL (entropy); n = 0 gives no
+ * gates. */
+nsg_status nsg_random_clifford(uint32_t n, const uint8_t* seed32, nsg_gate* out, size_t capacity,
+                               size_t* num_out);
+
+/* The seeded stream that measure, sample and random_clifford draw from: the
+ * first `count` 32-bit words of ChaCha with 12 rounds keyed by the 32 seed
+ * bytes (64-bit block counter from 0, stream id 0), the generator behind the
+ * reference's StdRng::from_seed (rand 0.8.5 / rand_chacha 0.3.1). */
+nsg_status nsg_random_words(const uint8_t* seed32, uint32_t* out, size_t count);
+
+/* Diagnostic: one ChaCha block (input words 0-15 → output words 0-15 after
+ * `rounds` rounds and the feed-forward addition), for known-answer tests of
+ * the stream above. */
+nsg_status nsg_debug_chacha_block(const uint32_t input[16], int32_t rounds, uint32_t output[16]);
+
 /* ------------------------------------------------------------------------ */
 /* Parity dump / checkpoint.  Writes every term as bool bytes:
  *   G, F, M: [term][row][col]   (num_terms · n · n bytes each)
@@ -316,14 +339,14 @@ nsg_status nsg_probe_int_ops(uint64_t iters, double* seconds, uint64_t* ops);
  * (crates/stabilizer-ch-form-rust/src/form/inner_product.rs:14-48) when
  * exp_value evaluates S_i against P·S_j (exp_value.rs:38-57).  Evaluates the
  * full χ×χ square with the production pair kernel; for parity tests. */
+nsg_status nsg_debug_pair_values(const nsg_state* state, const nsg_pauli* pauli,
+                                 uint8_t* k, int32_t* r);
+
 /* The device expansion of |T⟩^{⊗t} (construct_t_tensor_state,
  * crates/necstar/src/state/magic_states/t_state.rs:29-71; 1 ≤ t ≤ 64) as a
  * state of t qubits whose terms and coefficients are the expansion's, in its
  * order — for parity tests against the oracle. */
 nsg_status nsg_debug_t_tensor(uint32_t t, nsg_state** out);
-
-nsg_status nsg_debug_pair_values(const nsg_state* state, const nsg_pauli* pauli,
-                                 uint8_t* k, int32_t* r);
 
 #ifdef __cplusplus
 }

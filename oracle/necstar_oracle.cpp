@@ -21,18 +21,26 @@
 // (crates/necstar/src/state/types/scalar.rs:30-38).  Build with
 // -ffp-contract=off so no FMA contraction changes the rounding.
 //
-// Seeded RNG streams of the reference (rand 0.8.5 StdRng = ChaCha12,
-// rand_distr 0.4.3 Binomial, pinned in Cargo.lock) are third-party code that
-// is not part of the reference tree; measurement and sampling here use
-// xoshiro256** and an exact marginal, and are compared by distribution.
+// Seeded RNG streams of the reference come from third-party crates pinned in
+// Cargo.lock and not part of the reference tree: rand 0.8.5 StdRng
+// (= rand_chacha 0.3.1 ChaCha12Rng) and rand_distr 0.4.3 Binomial.  The
+// StdRng stream is restated here from the published ChaCha algorithm
+// (Bernstein 2008) in StdRng::from_seed's layout, together with rand's
+// conversions to f64 and to a u8 drawn from 0..=1; it is pinned to the
+// ChaCha known-answer vectors (RFC 7539 §2.3.2 and A.1, the eSTREAM 12-round
+// zero-key block).  With it, measure() and random_clifford() draw what the
+// reference draws for a given seed.  Binomial is not restated; sampling is
+// compared by distribution against the exact marginal.
 
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <complex>
 #include <cstdint>
 #include <cstring>
+#include <random>
 #include <map>
 #include <mutex>
 #include <stdexcept>
@@ -1162,42 +1170,191 @@ static std::vector<cplx> sd_statevector(const SDState& st) {
 }
 
 // ---------------------------------------------------------------------------
-// xoshiro256** (Blackman & Vigna), seeded from the 32 seed bytes.
+// rand 0.8.5 StdRng::from_seed(seed) = rand_chacha 0.3.1 ChaCha12Rng: the
+// ChaCha keystream (12 rounds) with key = seed, a 64-bit block counter from 0
+// and a zero 64-bit stream id, consumed as little-endian 32-bit words.
+static uint32_t chacha_rotl(uint32_t v, int c) { return (v << c) | (v >> (32 - c)); }
+
+static void chacha_block_words(const uint32_t input[16], int rounds, uint32_t out[16]) {
+    uint32_t w[16];
+    for (int i = 0; i < 16; i++) w[i] = input[i];
+    auto qr = [&w](int a, int b, int c, int d) {
+        w[a] += w[b]; w[d] ^= w[a]; w[d] = chacha_rotl(w[d], 16);
+        w[c] += w[d]; w[b] ^= w[c]; w[b] = chacha_rotl(w[b], 12);
+        w[a] += w[b]; w[d] ^= w[a]; w[d] = chacha_rotl(w[d], 8);
+        w[c] += w[d]; w[b] ^= w[c]; w[b] = chacha_rotl(w[b], 7);
+    };
+    for (int dr = 0; dr < rounds / 2; dr++) {
+        for (int col = 0; col < 4; col++) qr(col, col + 4, col + 8, col + 12);       // column round
+        for (int col = 0; col < 4; col++)                                            // diagonal round
+            qr(col, 4 + (col + 1) % 4, 8 + (col + 2) % 4, 12 + (col + 3) % 4);
+    }
+    for (int i = 0; i < 16; i++) out[i] = w[i] + input[i];
+}
+
 struct Rng {
-    uint64_t s[4];
-    static uint64_t splitmix(uint64_t& x) {
-        uint64_t z = (x += 0x9E3779B97F4A7C15ULL);
-        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
-        z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
-        return z ^ (z >> 31);
-    }
+    uint8_t key[32];
+    uint64_t block = 0;
+    uint8_t ks[64];  // current keystream block as bytes
+    int used = 64;
+
     explicit Rng(const uint8_t* seed32) {
-        uint64_t w[4] = {0, 0, 0, 0};
         if (seed32) {
-            for (int i = 0; i < 4; i++) std::memcpy(&w[i], seed32 + 8 * i, 8);
+            std::memcpy(key, seed32, 32);
         } else {
-            w[0] = (uint64_t)std::chrono::high_resolution_clock::now().time_since_epoch().count();
-        }
-        uint64_t x = w[0] ^ 0x6A09E667F3BCC909ULL;
-        for (int i = 0; i < 4; i++) {
-            x ^= w[i];
-            s[i] = splitmix(x);
+            std::random_device rd;
+            for (int i = 0; i < 32; i++) key[i] = (uint8_t)rd();
         }
     }
-    static uint64_t rotl(uint64_t x, int k) { return (x << k) | (x >> (64 - k)); }
-    uint64_t next() {
-        uint64_t r = rotl(s[1] * 5, 7) * 9;
-        uint64_t t = s[1] << 17;
-        s[2] ^= s[0];
-        s[3] ^= s[1];
-        s[1] ^= s[2];
-        s[0] ^= s[3];
-        s[2] ^= t;
-        s[3] = rotl(s[3], 45);
-        return r;
+    void refill() {
+        uint32_t in[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u};
+        for (int i = 0; i < 8; i++)
+            in[4 + i] = (uint32_t)key[4 * i] | (uint32_t)key[4 * i + 1] << 8 | (uint32_t)key[4 * i + 2] << 16 |
+                        (uint32_t)key[4 * i + 3] << 24;
+        in[12] = (uint32_t)block;
+        in[13] = (uint32_t)(block >> 32);
+        in[14] = in[15] = 0;
+        uint32_t out[16];
+        chacha_block_words(in, 12, out);
+        for (int i = 0; i < 16; i++)
+            for (int b = 0; b < 4; b++) ks[4 * i + b] = (uint8_t)(out[i] >> (8 * b));
+        block++;
+        used = 0;
     }
-    double uniform() { return (double)(next() >> 11) * (1.0 / 9007199254740992.0); }
+    uint32_t next_u32() {
+        if (used == 64) refill();
+        uint32_t v = (uint32_t)ks[used] | (uint32_t)ks[used + 1] << 8 | (uint32_t)ks[used + 2] << 16 |
+                     (uint32_t)ks[used + 3] << 24;
+        used += 4;
+        return v;
+    }
+    uint64_t next_u64() {  // rand_core BlockRng: low word first
+        uint64_t lo = next_u32();
+        uint64_t hi = next_u32();
+        return (hi << 32) | lo;
+    }
+    // rng.gen::<f64>(): 53 random bits scaled by 2^-53.
+    double uniform() { return std::ldexp((double)(next_u64() >> 11), -53); }
+    // rng.gen_range(0..=1) for u8: Lemire's widening multiply of a u32 draw by
+    // the range (2); the rejection zone is the whole u32 range here.
+    uint8_t range01() {
+        const uint64_t range = 2;
+        for (;;) {
+            const uint64_t prod = (uint64_t)next_u32() * range;
+            const uint32_t lo = (uint32_t)prod;
+            const uint32_t zone = UINT32_MAX - (uint32_t)(((uint64_t)UINT32_MAX - range + 1) % range);
+            if (lo <= zone) return (uint8_t)(prod >> 32);
+        }
+    }
 };
+
+static uint64_t splitmix(uint64_t& x) {  // SplitMix64 (pair sampling of the CPU timing)
+    uint64_t z = (x += 0x9E3779B97F4A7C15ULL);
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+
+// CliffordCircuit::random_clifford
+// (crates/stabilizer-ch-form-rust/src/circuit/random_clifford.rs:177-212).
+// sample_quantum_mallows :7-45
+static void rc_mallows(int n, Rng& rng, std::vector<uint8_t>& h, std::vector<size_t>& s) {
+    h.assign(n, 0);
+    s.assign(n, 0);
+    std::vector<size_t> avail;
+    for (int i = 0; i < n; i++) avail.push_back(i);
+    for (int i = 0; i < n; i++) {
+        const int m = n - i;
+        const double r = rng.uniform();
+        const double val = r * (std::pow(4.0, m) - 1.0) + 1.0;
+        const double cl = std::ceil(std::log2(val));
+        // `ceil_log as isize` saturates (NaN → 0)
+        long long ci = std::isnan(cl) ? 0 : (cl >= 9.2e18 ? LLONG_MAX : (long long)cl);
+        long long a = (ci > 2LL * m) ? 0 : (2LL * m + 1 - ci);
+        if (a <= 0) a = 1;
+        long long k1;
+        if (a <= m) {
+            h[i] = 1;
+            k1 = a;
+        } else {
+            h[i] = 0;
+            k1 = 2LL * m - a + 1;
+        }
+        // k1 - 1 wraps to usize::MAX when k1 = 0, which takes the pop branch
+        if (k1 >= 1 && (size_t)(k1 - 1) < avail.size()) {
+            s[i] = avail[(size_t)(k1 - 1)];
+            avail.erase(avail.begin() + (k1 - 1));
+        } else {
+            s[i] = avail.back();
+            avail.pop_back();
+        }
+    }
+}
+
+static std::vector<nsg_gate> rc_random_clifford(int n, const uint8_t* seed32) {
+    std::vector<nsg_gate> qc;
+    if (n == 0) return qc;
+    Rng rng(seed32);
+    // generate_clifford_params :62-122
+    std::vector<uint8_t> h;
+    std::vector<size_t> s;
+    rc_mallows(n, rng, h, s);
+    typedef std::vector<std::vector<uint8_t>> Mat;
+    Mat gamma1(n, std::vector<uint8_t>(n, 0)), gamma2 = gamma1, delta1 = gamma1, delta2 = gamma1;
+    for (int i = 0; i < n; i++) delta1[i][i] = delta2[i][i] = 1;
+    std::vector<uint8_t> pz(n), px(n);
+    for (int i = 0; i < n; i++) pz[i] = rng.range01();
+    for (int i = 0; i < n; i++) px[i] = rng.range01();
+    for (int i = 0; i < n; i++) {
+        gamma2[i][i] = rng.range01();
+        if (h[i] == 1) gamma1[i][i] = rng.range01();
+    }
+    for (int i = 1; i < n; i++)
+        for (int j = 0; j < i; j++) {
+            uint8_t b2 = rng.range01();
+            gamma2[i][j] = b2;
+            gamma2[j][i] = b2;
+            delta2[i][j] = rng.range01();
+            const bool hi = h[i] == 1, hj = h[j] == 1;
+            const size_t si = s[i], sj = s[j];
+            if (((si < sj || hj) && hi) || (hj && sj < si)) {
+                uint8_t b = rng.range01();
+                gamma1[i][j] = b;
+                gamma1[j][i] = b;
+            }
+            if ((si < sj || hj) && (si > sj || !hi) && (hj || !hi)) delta1[i][j] = rng.range01();
+        }
+    // apply_hadamard_free_layer :125-165, apply_permutation_layer :168-180
+    auto layer = [&](const Mat& gamma, const Mat& delta, bool paulis) {
+        for (int j = 0; j < n; j++)
+            for (int i = j + 1; i < n; i++)
+                if (delta[i][j] == 1) qc.push_back({NSG_GATE_CX, (uint32_t)j, (uint32_t)i, 0});
+        for (int i = 0; i < n; i++) {
+            if (gamma[i][i] == 1) qc.push_back({NSG_GATE_S, (uint32_t)i, 0, 0});
+            for (int j = 0; j < i; j++)
+                if (gamma[i][j] == 1) qc.push_back({NSG_GATE_CZ, (uint32_t)i, (uint32_t)j, 0});
+        }
+        if (paulis)
+            for (int i = 0; i < n; i++) {
+                if (pz[i] == 1 && px[i] == 1) qc.push_back({NSG_GATE_Y, (uint32_t)i, 0, 0});
+                else if (pz[i] == 1) qc.push_back({NSG_GATE_Z, (uint32_t)i, 0, 0});
+                else if (px[i] == 1) qc.push_back({NSG_GATE_X, (uint32_t)i, 0, 0});
+            }
+    };
+    layer(gamma2, delta2, true);
+    std::vector<size_t> p;
+    for (int i = 0; i < n; i++) p.push_back(i);
+    for (int i = 0; i < n; i++)
+        if (p[i] != s[i]) {
+            size_t j = std::find(p.begin(), p.end(), s[i]) - p.begin();
+            qc.push_back({NSG_GATE_SWAP, (uint32_t)i, (uint32_t)j, 0});
+            std::swap(p[i], p[j]);
+        }
+    for (int i = 0; i < n; i++)
+        if (h[i] == 1) qc.push_back({NSG_GATE_H, (uint32_t)i, 0, 0});
+    layer(gamma1, delta1, false);
+    return qc;
+}
 
 // measure (stabilizer_decomposed_state/measurement.rs:10-103)
 static std::vector<uint8_t> sd_measure(SDState& st, const std::vector<int>& qargs, const uint8_t* seed) {
@@ -1492,6 +1649,35 @@ int orc_measure(void* st, const uint32_t* qargs, size_t k, const uint8_t* seed32
     ORC_CATCH
 }
 
+int orc_random_clifford(uint32_t n, const uint8_t* seed32, nsg_gate* out, size_t cap, size_t* nout) {
+    ORC_TRY
+    std::vector<nsg_gate> g = rc_random_clifford((int)n, seed32);
+    *nout = g.size();
+    if (g.size() > cap) fail(NSG_ERR_BUFFER_TOO_SMALL, (int64_t)g.size(), (int64_t)cap);
+    std::copy(g.begin(), g.end(), out);
+    ORC_CATCH
+}
+
+int orc_random_words(const uint8_t* seed32, uint32_t* out, size_t count) {
+    ORC_TRY
+    Rng rng(seed32);
+    for (size_t i = 0; i < count; i++) out[i] = rng.next_u32();
+    ORC_CATCH
+}
+
+int orc_random_doubles(const uint8_t* seed32, double* out, size_t count) {
+    ORC_TRY
+    Rng rng(seed32);
+    for (size_t i = 0; i < count; i++) out[i] = rng.uniform();
+    ORC_CATCH
+}
+
+int orc_chacha_block(const uint32_t* input, int32_t rounds, uint32_t* out) {
+    ORC_TRY
+    chacha_block_words(input, rounds, out);
+    ORC_CATCH
+}
+
 // Exact marginal of qargs: writes up to `cap` (outcome, probability) pairs.
 int orc_marginal(void* stv, const uint32_t* qargs, size_t k, uint64_t* outcomes, double* probs, size_t cap,
                  size_t* nout) {
@@ -1594,7 +1780,7 @@ int orc_time_pairs(void* stv, const nsg_pauli* p, uint64_t num_pairs, uint64_t s
                 while (true) {
                     uint64_t idx = next.fetch_add(1);
                     if (idx >= num_pairs) break;
-                    uint64_t h1 = Rng::splitmix(x), h2 = Rng::splitmix(x);
+                    uint64_t h1 = splitmix(x), h2 = splitmix(x);
                     size_t i = (size_t)(h1 % chi), j = (size_t)(h2 % chi);
                     if (j < i) std::swap(i, j);
                     ChForm ev = st->stabs[i];

@@ -63,6 +63,10 @@ def lib():
         L.orc_project_normalized.argtypes = [vp, C.c_uint32, C.c_int32]
         L.orc_discard.argtypes = [vp, C.c_uint32]
         L.orc_measure.argtypes = [vp, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
+        L.orc_random_clifford.argtypes = [C.c_uint32, C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(C.c_size_t)]
+        L.orc_random_words.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+        L.orc_random_doubles.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+        L.orc_chacha_block.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
         L.orc_marginal.argtypes = [vp, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_size_t,
                                    C.POINTER(C.c_size_t)]
         L.orc_to_statevector.argtypes = [vp, C.c_void_p, C.c_size_t]
@@ -248,6 +252,39 @@ class OracleState:
         sec, cs = C.c_double(), C.c_double()
         _check(lib().orc_time_pairs(self._h, C.byref(st), num_pairs, seed, threads, C.byref(sec), C.byref(cs)))
         return sec.value, cs.value
+
+
+def random_clifford(n: int, seed: bytes | None) -> np.ndarray:
+    """CliffordCircuit::random_clifford (random_clifford.rs:177-212) as gate rows (op, q0, q1, q2)."""
+    cap = 2 * n * n + 3 * n + 1
+    out = np.zeros((cap, 4), np.uint32)
+    sd = np.frombuffer(seed, dtype=np.uint8).copy() if seed is not None else None
+    nout = C.c_size_t()
+    _check(lib().orc_random_clifford(n, _ptr(sd) if sd is not None else None, _ptr(out), cap, C.byref(nout)))
+    return out[:nout.value].copy()
+
+
+def random_words(seed: bytes, count: int) -> np.ndarray:
+    """The first `count` 32-bit words of StdRng::from_seed(seed)."""
+    sd = np.frombuffer(seed, dtype=np.uint8).copy()
+    out = np.zeros(count, np.uint32)
+    _check(lib().orc_random_words(_ptr(sd), _ptr(out), count))
+    return out
+
+
+def random_doubles(seed: bytes, count: int) -> np.ndarray:
+    """The first `count` rng.gen::<f64>() draws of StdRng::from_seed(seed)."""
+    sd = np.frombuffer(seed, dtype=np.uint8).copy()
+    out = np.zeros(count, np.float64)
+    _check(lib().orc_random_doubles(_ptr(sd), _ptr(out), count))
+    return out
+
+
+def chacha_block(words, rounds: int) -> list[int]:
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    out = np.zeros(16, np.uint32)
+    _check(lib().orc_chacha_block(_ptr(w), rounds, _ptr(out)))
+    return [int(x) for x in out]
 
 
 def dense_simulate(n: int, gates) -> np.ndarray:

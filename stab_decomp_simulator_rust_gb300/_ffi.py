@@ -83,6 +83,9 @@ def load(path: str | None = None):
     L.nsg_export_terms.argtypes = [vp] + [vp] * 11
     L.nsg_debug_pair_values.argtypes = [vp, vp, vp, vp]
     L.nsg_debug_t_tensor.argtypes = [u32, P(vp)]
+    L.nsg_random_clifford.argtypes = [u32, vp, vp, sz, P(sz)]
+    L.nsg_random_words.argtypes = [vp, vp, sz]
+    L.nsg_debug_chacha_block.argtypes = [vp, i32, vp]
     L.nsg_profile_enable.argtypes = [i32]
     L.nsg_profile_read.argtypes = [P(dbl), P(u64), P(u64)]
     L.nsg_probe_int_ops.argtypes = [u64, P(dbl), P(u64)]

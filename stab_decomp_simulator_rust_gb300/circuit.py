@@ -5,11 +5,22 @@ python/necstar/gate.pyi; Rust crates/necstar/src/circuit/mod.rs:53-56 and
 circuit/gates.rs:7-42).  A circuit is a gate list; the gate opcodes are those
 of include/necstar_gpu.h.  Nothing is validated here: like the reference,
 qubit indices are checked when the circuit is compiled.
+
+Circuit ingestion follows crates/necstar/src/circuit/parser.rs: an OpenQASM
+2.0 subset read line by line (one register, the gates h x y z s sdg sx sxdg
+t tdg cx cz swap ccx, ``measure`` lines ignored with a warning, anything
+else an error) and written back in the same form; ``random_clifford`` draws
+a uniformly random Clifford circuit with the library's seeded generator.
 """
 from __future__ import annotations
 
+import ctypes as C
+import re
+import sys
+
 import numpy as np
 
+from ._ffi import NecstarError
 from .workloads import OP
 
 _NAMES = {v: k for k, v in OP.items()}
@@ -17,9 +28,22 @@ _DISPLAY = {"H": "H", "X": "X", "Y": "Y", "Z": "Z", "S": "S", "SDG": "Sdg", "SQR
             "SQRT_XDG": "SqrtXdg", "CX": "CX", "CZ": "CZ", "SWAP": "Swap", "T": "T", "TDG": "Tdg", "CCX": "CCX"}
 _ARITY = {"H": 1, "X": 1, "Y": 1, "Z": 1, "S": 1, "SDG": 1, "SQRT_X": 1, "SQRT_XDG": 1,
           "CX": 2, "CZ": 2, "SWAP": 2, "T": 1, "TDG": 1, "CCX": 3}
-_ALIASES = {"h": "H", "x": "X", "y": "Y", "z": "Z", "s": "S", "sdg": "SDG", "sx": "SQRT_X", "sqrt_x": "SQRT_X",
-            "sxdg": "SQRT_XDG", "sqrt_xdg": "SQRT_XDG", "cx": "CX", "cnot": "CX", "cz": "CZ", "swap": "SWAP",
-            "t": "T", "tdg": "TDG", "ccx": "CCX", "toffoli": "CCX"}
+# QuantumCircuit.apply_gate(name, qubits) of the Python layer
+# (python/src/circuit.rs:90-186): case-insensitive names, the arity message
+# of each gate; CCX is not reachable by name there.
+_BY_NAME = {"h": ("H", "H gate requires 1 qubit index."), "x": ("X", "X gate requires 1 qubit index."),
+            "y": ("Y", "Y gate requires 1 qubit index."), "z": ("Z", "Z gate requires 1 qubit index."),
+            "s": ("S", "S gate requires 1 qubit index."), "sdg": ("SDG", "Sdg gate requires 1 qubit index."),
+            "sqrtx": ("SQRT_X", "SqrtX gate requires 1 qubit index."),
+            "sqrtxdg": ("SQRT_XDG", "SqrtXdg gate requires 1 qubit index."),
+            "t": ("T", "T gate requires 1 qubit index."), "tdg": ("TDG", "Tdg gate requires 1 qubit index."),
+            "cx": ("CX", "CX gate requires 2 qubit indices (control, target)."),
+            "cnot": ("CX", "CX gate requires 2 qubit indices (control, target)."),
+            "cz": ("CZ", "CZ gate requires 2 qubit indices."), "swap": ("SWAP", "SWAP gate requires 2 qubit indices.")}
+# OpenQASM mnemonics (QuantumGate::to_qasm_str, crates/necstar/src/circuit/gates.rs:235-257)
+_QASM = {"H": "h", "X": "x", "Y": "y", "Z": "z", "S": "s", "SDG": "sdg", "SQRT_X": "sx", "SQRT_XDG": "sxdg",
+         "T": "t", "TDG": "tdg", "CX": "cx", "CZ": "cz", "SWAP": "swap", "CCX": "ccx"}
+_FROM_QASM = {v: k for k, v in _QASM.items()}
 
 
 class QuantumGate:
@@ -128,16 +152,19 @@ class QuantumCircuit:
         return np.asarray(self._rows, dtype=np.uint32).reshape(-1, 4)
 
     def apply_gate(self, gate, qubits=None) -> None:
-        """``apply_gate(QuantumGate)`` or ``apply_gate(name, qubits)`` (circuit.pyi:141)."""
+        """``apply_gate(name, qubits)`` (python/necstar/circuit.pyi:141) or ``apply_gate(QuantumGate)``."""
         if isinstance(gate, QuantumGate):
             self._rows.append(gate.row())
             return
-        key = _ALIASES.get(str(gate).lower(), str(gate).upper())
-        if key not in OP:
-            raise ValueError(f"Unknown gate name: {gate}")
-        qs = list(qubits or [])
+        entry = _BY_NAME.get(str(gate).lower())
+        if entry is None:
+            raise ValueError(f"Unknown gate name: '{gate}'")
+        key, arity_msg = entry
+        qs = [int(q) for q in (qubits or [])]
+        if any(q < 0 for q in qs):
+            raise OverflowError("can't convert negative int to unsigned")
         if len(qs) != _ARITY[key]:
-            raise ValueError(f"Gate {gate} expects {_ARITY[key]} qubits, got {len(qs)}")
+            raise ValueError(arity_msg)
         self._rows.append(QuantumGate(OP[key], qs).row())
 
     def apply_gates(self, gates) -> None:
@@ -162,5 +189,171 @@ class QuantumCircuit:
     def apply_swap(self, a, b): self._rows.append((OP["SWAP"], a, b, 0))
     def apply_ccx(self, c1, c2, t): self._rows.append((OP["CCX"], c1, c2, t))
 
-    def __str__(self) -> str:
-        return f"QuantumCircuit(num_qubits={self._n}, num_gates={len(self._rows)})"
+    def tensor(self, other: "QuantumCircuit") -> "QuantumCircuit":
+        """self ⊗ other: other's gates act on qubits shifted by self.num_qubits
+        (QuantumCircuit::tensor, crates/necstar/src/circuit/mod.rs:253-270)."""
+        c = QuantumCircuit(self._n + other._n)
+        off = self._n
+        c._rows = list(self._rows)
+        for op, q0, q1, q2 in other._rows:
+            k = _ARITY[_NAMES[op]]
+            c._rows.append((op, q0 + off, q1 + off if k > 1 else q1, q2 + off if k > 2 else q2))
+        return c
+
+    # ---- OpenQASM 2.0 (crates/necstar/src/circuit/parser.rs) ----
+    @staticmethod
+    def from_qasm_str(qasm: str) -> "QuantumCircuit":
+        """parser.rs:17-186; every failure is a ValueError "Failed to parse QASM string: …"
+        (python/src/circuit.rs:53-60)."""
+        try:
+            return _parse_qasm(qasm)
+        except _QasmError as e:
+            raise _qasm_exc(NecstarError, f"Failed to parse QASM string: {e}") from None
+
+    @staticmethod
+    def from_qasm_file(path: str) -> "QuantumCircuit":
+        """parser.rs:191-201; every failure (unreadable file or bad content) is a
+        FileNotFoundError "Failed to read QASM file: …" (python/src/circuit.rs:43-51)."""
+        try:
+            try:
+                with open(path, "rb") as f:
+                    raw = f.read()
+            except OSError as e:
+                raise _QasmError(f"Failed to read file '{path}': {_os_message(e)}") from None
+            try:
+                text = raw.decode("utf-8")
+            except UnicodeDecodeError:
+                raise _QasmError(f"Failed to read file '{path}': stream did not contain valid UTF-8") from None
+            return _parse_qasm(text)
+        except _QasmError as e:
+            raise _qasm_exc(QasmFileError, f"Failed to read QASM file: {e}") from None
+
+    def to_qasm_str(self, reg_name: str) -> str:
+        """parser.rs:203-214: header, register, one line per gate, no final newline."""
+        lines = ["OPENQASM 2.0;", 'include "qelib1.inc";', f"qreg {reg_name}[{self._n}];"]
+        for op, q0, q1, q2 in self._rows:
+            name = _NAMES[op]
+            args = [q0, q1, q2][:_ARITY[name]]
+            lines.append(f"{_QASM[name]} " + ", ".join(f"{reg_name}[{q}]" for q in args) + ";")
+        return "\n".join(lines)
+
+    def to_qasm_file(self, path: str, reg_name: str) -> None:
+        """parser.rs:221-230; a write failure is a ValueError "Failed to write QASM file: IO error: …"."""
+        text = self.to_qasm_str(reg_name)
+        try:
+            with open(path, "wb") as f:
+                f.write(text.encode("utf-8"))
+        except OSError as e:
+            raise NecstarError(_IO_ERR, f"Failed to write QASM file: IO error: {_os_message(e)}", [-1, -1, -1]) \
+                from None
+
+    @staticmethod
+    def random_clifford(n: int, seed=None) -> "QuantumCircuit":
+        """A uniformly random n-qubit Clifford circuit (QuantumCircuit::random_clifford,
+        crates/necstar/src/circuit/mod.rs:289-291): the Bravyi–Maslov canonical form drawn
+        by nsg_random_clifford from the seeded stream (seeds as in python/src/utils.rs)."""
+        from . import _ffi
+        from .state import seed_bytes
+        n = int(n)
+        if n < 0:
+            raise OverflowError("can't convert negative int to unsigned")
+        sd = seed_bytes(seed)
+        cap = 2 * n * n + 3 * n
+        out = np.zeros((max(cap, 1), 4), dtype=np.uint32)
+        nout = C.c_size_t()
+        _ffi.check(_ffi.load().nsg_random_clifford(
+            n, sd.ctypes.data_as(C.c_void_p) if sd is not None else None,
+            out.ctypes.data_as(C.c_void_p), cap, C.byref(nout)))
+        return QuantumCircuit.from_gate_array(n, out[:nout.value])
+
+    def __str__(self) -> str:  # QuantumCircuit Display (crates/necstar/src/circuit/mod.rs:326-338)
+        return f"QuantumCircuit(num_qubits={self._n}) [" + ", ".join(str(g) for g in self.gates) + "]"
+
+    __repr__ = __str__
+
+
+# ---------------------------------------------------------------------------
+# OpenQASM 2.0 reader (parser.rs:17-186).  Each line is trimmed; blank lines,
+# "//" comments and lines starting with OPENQASM or include are skipped; a
+# qreg declaration (exactly one) sets the width; "measure" lines are ignored
+# with a warning on stderr; otherwise the line must contain a 3-, 2- or
+# 1-qubit gate application of a known name (tried in that order) or it is an
+# error.  Matching is a search within the line, as the reference's regexes do.
+_IDENT = r"[a-zA-Z][a-zA-Z0-9_]*"
+_QREG = re.compile(r"qreg\s+(" + _IDENT + r")\s*\[\s*(\d+)\s*\]\s*;")
+
+
+def _gate_pattern(k: int) -> re.Pattern:
+    arg = r"(" + _IDENT + r")\[(\d+)\]"
+    return re.compile(r"([a-z_]+)\s+" + r",\s*".join([arg] * k) + r"\s*;")
+
+
+_GATE_RE = {k: _gate_pattern(k) for k in (3, 2, 1)}
+# Unicode White_Space (Rust's str::trim)
+_WS = "\t\n\x0b\x0c\r \x85\xa0\u1680\u2000\u2001\u2002\u2003\u2004\u2005\u2006\u2007\u2008\u2009\u200a" \
+      "\u2028\u2029\u202f\u205f\u3000"
+_QASM_ERR = 19  # NSG_ERR_QASM_PARSING
+_IO_ERR = 20    # NSG_ERR_IO
+
+
+class _QasmError(Exception):
+    def __str__(self) -> str:  # Error::QasmParsingError Display (crates/necstar/src/error/mod.rs:73)
+        return f"QASM parsing error: {self.args[0]}"
+
+
+def _os_message(e: OSError) -> str:  # std::io::Error Display for an OS error
+    return f"{e.strerror} (os error {e.errno})" if e.errno is not None else str(e)
+
+
+def _usize(text: str, line: str, what: str) -> int:
+    """`str::parse::<usize>()` with its failure messages."""
+    if not text.isascii():
+        raise _QasmError(f"Invalid {what} in line: '{line}' (invalid digit found in string)")
+    v = int(text)
+    if v >= 1 << 64:
+        raise _QasmError(f"Invalid {what} in line: '{line}' (number too large to fit in target type)")
+    return v
+
+
+def _parse_qasm(qasm: str) -> "QuantumCircuit":
+    n = None
+    rows = []
+    for num, raw in enumerate(qasm.split("\n")):
+        line = raw.strip(_WS)
+        if not line or line.startswith("//") or line.startswith("OPENQASM") or line.startswith("include"):
+            continue
+        m = _QREG.search(line)
+        if m:
+            if n is not None:
+                raise _QasmError("Multiple qreg declarations are not supported.")
+            n = _usize(m.group(2), line, "qreg size")
+            continue
+        if line.startswith("measure"):
+            sys.stderr.write(f"[Warning] Line {num + 1}: `measure` operation is ignored by the parser.\n")
+            continue
+        done = False
+        for k in (3, 2, 1):
+            m = _GATE_RE[k].search(line)
+            if not m:
+                continue
+            key = _FROM_QASM.get(m.group(1))
+            if key is None or _ARITY[key] != k:
+                continue
+            qs = [_usize(m.group(3 + 2 * a), line, "qubit index") for a in range(k)] + [0] * (3 - k)
+            rows.append((OP[key], qs[0], qs[1], qs[2]))
+            done = True
+            break
+        if not done:
+            raise _QasmError(f"Unrecognized or malformed line: {line}")
+    if n is None:
+        raise _QasmError("qreg declaration not found in QASM string.")
+    return QuantumCircuit.from_gate_array(n, np.asarray(rows, dtype=np.uint64).reshape(-1, 4))
+
+
+def _qasm_exc(cls, message: str):
+    return cls(_QASM_ERR, message, [-1, -1, -1])
+
+
+class QasmFileError(NecstarError, FileNotFoundError):
+    """from_qasm_file's failure: a FileNotFoundError like the reference's Python layer
+    (python/src/circuit.rs:45-47), and a NecstarError like every other failure here."""

@@ -23,6 +23,7 @@
 #include "chform_host.hpp"
 #include "device_state.hpp"
 #include "host_rng.hpp"
+#include "random_clifford.hpp"
 
 using namespace nsg;
 
@@ -2054,6 +2055,42 @@ nsg_status nsg_probe_int_ops(uint64_t iters, double* seconds, uint64_t* ops) {
     cudaStreamDestroy(st);
     *seconds = ms * 1e-3;
     *ops = (uint64_t)blocks * threads * iters * 16 * 8;
+    API_END
+}
+
+nsg_status nsg_random_clifford(uint32_t n, const uint8_t* seed32, nsg_gate* out, size_t capacity, size_t* num_out) {
+    API_BEGIN
+    need(num_out, "num_out");
+    *num_out = 0;
+    const uint64_t bound = random_clifford_max_gates(n);
+    if (bound) need(out, "out");
+    if (capacity < bound)
+        raise(NSG_ERR_BUFFER_TOO_SMALL, (int64_t)bound, (int64_t)capacity,
+              "capacity %zu is below the %llu gates a random Clifford on %u qubits may need", capacity,
+              (unsigned long long)bound, n);
+    HostRng rng(seed32);
+    const std::vector<nsg_gate> g = random_clifford_gates(n, rng);
+    std::copy(g.begin(), g.end(), out);
+    *num_out = g.size();
+    API_END
+}
+
+nsg_status nsg_random_words(const uint8_t* seed32, uint32_t* out, size_t count) {
+    API_BEGIN
+    need(seed32, "seed32");
+    if (count) need(out, "out");
+    HostRng rng(seed32);
+    for (size_t i = 0; i < count; i++) out[i] = rng.next_u32();
+    API_END
+}
+
+nsg_status nsg_debug_chacha_block(const uint32_t input[16], int32_t rounds, uint32_t output[16]) {
+    API_BEGIN
+    need(input, "input");
+    need(output, "output");
+    if (rounds <= 0 || rounds % 2 != 0 || rounds > 64)
+        raise(NSG_ERR_INVALID_ARGUMENT, rounds, -1, "rounds must be a positive even number up to 64, got %d", rounds);
+    ChaChaCore::block(input, rounds, output);
     API_END
 }
 

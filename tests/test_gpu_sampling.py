@@ -106,3 +106,27 @@ def test_measure_all_known_answer(gpu_pkg):
         assert k in (0, 1, 2, 7)
         sv = st.to_statevector()
         assert abs(abs(sv[k]) - 1.0) < 1e-9
+
+
+def test_measure_draws_the_reference_stream(gpu_pkg, oracle):
+    # measure() takes one rng.gen::<f64>() per measured qubit from
+    # StdRng::from_seed(seed) and returns 1 iff the draw is not below
+    # p0 / (p0 + p1) (measurement.rs:34-103).  On |+⟩^n every p0 is 1/2, so
+    # the outcomes are fixed by the stream alone.
+    from conftest import OP
+    n = 12
+    plus = [(OP["H"], q, 0, 0) for q in range(n)]
+    for s in range(6):
+        seed = bytes([17 * s + 1]) * 32
+        st = gpu_pkg.QuantumState.from_gates(n, plus)
+        u = oracle.random_doubles(seed, n)
+        assert st.measure(list(range(n)), seed=seed) == [bool(x >= 0.5) for x in u]
+    # On Clifford+T states the outcomes equal the oracle's for the same seed.
+    for n, nc, nt, gseed in ((6, 150, 7, 231), (9, 220, 9, 232)):
+        gates = random_full_circuit(n, nc, nt, gseed)
+        qargs = list(range(n))[::-1]
+        for s in range(4):
+            seed = (gseed * 1000 + s).to_bytes(8, "little") + bytes(24)
+            ref = oracle.OracleState.from_circuit(n, gates)
+            st = gpu_pkg.QuantumState.from_gates(n, gates)
+            assert st.measure(qargs, seed=seed) == ref.measure(qargs, seed)

@@ -95,7 +95,7 @@ def test_circuit_builder():
     c.apply_h(0)
     c.apply_cx(0, 1)
     c.apply_t(2)
-    c.apply_gate("ccx", [0, 1, 2])
+    c.apply_ccx(0, 1, 2)
     c.apply_gate(QuantumGate.sdg(1))
     assert c.num_qubits == 3 and c.num_gates == 5
     assert [str(g) for g in c.gates] == ["H(0)", "CX(0, 1)", "T(2)", "CCX(0, 1, 2)", "Sdg(1)"]
