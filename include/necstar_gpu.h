@@ -282,6 +282,16 @@ nsg_status nsg_sample(const nsg_state* state, const uint32_t* qargs, size_t num_
  * values as interleaved (re, im); n ≤ 28. */
 nsg_status nsg_to_statevector(const nsg_state* state, double* out, size_t capacity_complex);
 
+/* |a⟩ ⊗ |b⟩ as a new state of n_a + n_b ≤ 128 qubits (b's qubits follow a's):
+ * term i·χ_b + j is the CH-form kron of a's term i and b's term j with the
+ * product coefficient, in the order of StabilizerDecomposedState::kron
+ * (crates/necstar/src/state/stabilizer_decomposed_state/kron.rs:7-22, with
+ * StabilizerCHForm::kron, crates/stabilizer-ch-form-rust/src/form/kron.rs:12-59;
+ * crate-internal in the reference, where it builds the magic states).  The
+ * global factors multiply (the reference's result has factor 1, which is the
+ * product wherever it calls it).  Both states must be on one device. */
+nsg_status nsg_state_kron(const nsg_state* a, const nsg_state* b, nsg_state** out);
+
 /* QuantumCircuit::random_clifford (crates/necstar/src/circuit/mod.rs:289-291
  * → crates/stabilizer-ch-form-rust/src/circuit/random_clifford.rs:177-212):
  * a uniformly random n-qubit Clifford as a gate list (Bravyi–Maslov canonical

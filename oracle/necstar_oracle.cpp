@@ -1538,6 +1538,12 @@ int orc_state_from_terms(uint32_t n, uint64_t chi, const uint8_t* G, const uint8
 
 void orc_state_free(void* st) { delete (SDState*)st; }
 
+int orc_state_kron(void* a, void* b, void** out) {
+    ORC_TRY
+    *out = new SDState(sd_kron(*(SDState*)a, *(SDState*)b));
+    ORC_CATCH
+}
+
 int orc_state_clone(void* st, void** out) {
     ORC_TRY
     *out = new SDState(*(SDState*)st);

@@ -50,6 +50,7 @@ def lib():
         L.orc_state_from_terms.argtypes = [C.c_uint32, C.c_uint64] + [C.c_void_p] * 10 + [C.c_void_p, C.POINTER(vp)]
         L.orc_state_free.argtypes = [vp]
         L.orc_state_clone.argtypes = [vp, C.POINTER(vp)]
+        L.orc_state_kron.argtypes = [vp, vp, C.POINTER(vp)]
         L.orc_num_qubits.argtypes = [vp, C.POINTER(C.c_uint32)]
         L.orc_stabilizer_rank.argtypes = [vp, C.POINTER(C.c_uint64)]
         L.orc_export_terms.argtypes = [vp] + [C.c_void_p] * 11
@@ -147,6 +148,12 @@ class OracleState:
         gf = np.ascontiguousarray(d.get("global_factor", [1.0, 0.0]), dtype=np.float64)
         h = C.c_void_p()
         _check(lib().orc_state_from_terms(n, chi, *[_ptr(a) for a in arrs], _ptr(r), _ptr(z), _ptr(gf), C.byref(h)))
+        return OracleState(h)
+
+    def kron(self, other: "OracleState") -> "OracleState":
+        """StabilizerDecomposedState::kron (stabilizer_decomposed_state/kron.rs:7-22)."""
+        h = C.c_void_p()
+        _check(lib().orc_state_kron(self._h, other._h, C.byref(h)))
         return OracleState(h)
 
     def clone(self) -> "OracleState":

@@ -83,6 +83,7 @@ def load(path: str | None = None):
     L.nsg_export_terms.argtypes = [vp] + [vp] * 11
     L.nsg_debug_pair_values.argtypes = [vp, vp, vp, vp]
     L.nsg_debug_t_tensor.argtypes = [u32, P(vp)]
+    L.nsg_state_kron.argtypes = [vp, vp, P(vp)]
     L.nsg_random_clifford.argtypes = [u32, vp, vp, sz, P(sz)]
     L.nsg_random_words.argtypes = [vp, vp, sz]
     L.nsg_debug_chacha_block.argtypes = [vp, i32, vp]

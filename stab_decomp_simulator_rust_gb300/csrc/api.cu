@@ -2058,6 +2058,35 @@ nsg_status nsg_probe_int_ops(uint64_t iters, double* seconds, uint64_t* ops) {
     API_END
 }
 
+nsg_status nsg_state_kron(const nsg_state* a, const nsg_state* b, nsg_state** out) {
+    API_BEGIN
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    *out = nullptr;
+    if (a->device != b->device)
+        raise(NSG_ERR_INVALID_ARGUMENT, a->device, b->device, "the two states live on different devices");
+    DeviceScope ds_(a->device);
+    const int n = a->t.n + b->t.n;
+    if (n > 128) raise(NSG_ERR_TOO_WIDE, n, 128, "width %d exceeds 128", n);
+    const int64_t ca = a->t.chi, cb = b->t.chi;
+    if (ca && cb > (int64_t)(INT64_MAX / 256) / ca)
+        raise(NSG_ERR_OUT_OF_MEMORY, ca, cb, "%lld x %lld terms do not fit", (long long)ca, (long long)cb);
+    auto o = std::make_unique<nsg_state>();
+    o->init_stream();
+    CK(cudaStreamSynchronize(a->st));  // the inputs' pending work, then ours
+    if (b != a) CK(cudaStreamSynchronize(b->st));
+    o->t.alloc(n, ca * cb, o->st);
+    o->t.chi = ca * cb;
+    CK(launch_kron(a->t.view(), b->t.view(), o->t.view(), o->st));
+    // global factors multiply (kron.rs builds its result with factor 1; both are 1 wherever the reference calls it)
+    o->gf_re = a->gf_re * b->gf_re - a->gf_im * b->gf_im;
+    o->gf_im = a->gf_re * b->gf_im + a->gf_im * b->gf_re;
+    CK(cudaStreamSynchronize(o->st));
+    *out = o.release();
+    API_END
+}
+
 nsg_status nsg_random_clifford(uint32_t n, const uint8_t* seed32, nsg_gate* out, size_t capacity, size_t* num_out) {
     API_BEGIN
     need(num_out, "num_out");

@@ -132,6 +132,10 @@ cudaError_t launch_unpack(const TermsView& t, uint8_t* G, uint8_t* F, uint8_t* M
 cudaError_t launch_pack(TermsView t, const uint8_t* G, const uint8_t* F, const uint8_t* M,
                         const uint8_t* gam, const uint8_t* v, const uint8_t* s, cudaStream_t st);
 
+// A ⊗ B term by term (output term i·χ_B + j), into O (width n_A + n_B, χ_A·χ_B
+// terms allocated by the caller).
+cudaError_t launch_kron(TermsView A, TermsView B, TermsView O, cudaStream_t st);
+
 // Bra frames (U_C^{-1} tableau) of every term; n ≤ 64.
 cudaError_t launch_frames(const TermsView& t, FrameView fr, cudaStream_t st);
 

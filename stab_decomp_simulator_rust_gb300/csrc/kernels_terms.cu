@@ -629,6 +629,70 @@ cudaError_t launch_pack(TermsView t, const uint8_t* G, const uint8_t* F, const u
     return cudaGetLastError();
 }
 
+// Word k of a width-n bit row with the bits at and above n cleared.
+__device__ __forceinline__ uint64_t row_word(const uint64_t* src, int n, int k) {
+    const int lo = 64 * k;
+    if (n <= lo) return 0;
+    return n >= lo + 64 ? src[k] : src[k] & ((1ULL << (n - lo)) - 1);
+}
+
+// Word w of (row << sh) for a width-n row held in words.
+__device__ __forceinline__ uint64_t shifted_word(const uint64_t* src, int n, int sh, int w) {
+    const int ws = sh >> 6, bs = sh & 63;
+    const int hi = w - ws, lo = hi - 1;
+    uint64_t x = hi >= 0 ? row_word(src, n, hi) << bs : 0;
+    if (bs && lo >= 0) x |= row_word(src, n, lo) >> (64 - bs);
+    return x;
+}
+
+// Term (i, j) ↦ i·χ_B + j of A ⊗ B (stabilizer_decomposed_state/kron.rs:7-22
+// with form/kron.rs:12-59): G, F, M block-diagonal, γ, v, s concatenated (B's
+// qubits after A's), phase factors multiplied, coefficients multiplied.  One
+// thread per (output term, row slot), as pack_kernel.
+__global__ void kron_kernel(TermsView A, TermsView B, TermsView O) {
+    const int64_t total = O.chi * O.R;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t term = t / O.R;
+        const int r = (int)(t % O.R);
+        const int64_t i = term / B.chi, j = term % B.chi;
+        const uint64_t *g = nullptr, *f = nullptr, *m = nullptr;
+        int width = 0, sh = 0;
+        if (r < A.n) {
+            const size_t o = ((size_t)i * A.R + r) * A.W;
+            g = A.G + o; f = A.F + o; m = A.M + o; width = A.n;
+        } else if (r < O.n) {
+            const size_t o = ((size_t)j * B.R + (r - A.n)) * B.W;
+            g = B.G + o; f = B.F + o; m = B.M + o; width = B.n; sh = A.n;
+        }
+        for (int w = 0; w < O.W; w++) {
+            const size_t idx = ((size_t)term * O.R + r) * O.W + w;
+            O.G[idx] = g ? shifted_word(g, width, sh, w) : 0;
+            O.F[idx] = f ? shifted_word(f, width, sh, w) : 0;
+            O.M[idx] = m ? shifted_word(m, width, sh, w) : 0;
+        }
+        if (r < O.W) {  // vectors: word r of the term
+            const size_t oa = (size_t)i * A.W, ob = (size_t)j * B.W, oo = (size_t)term * O.W + r;
+            O.V[oo] = shifted_word(A.V + oa, A.n, 0, r) | shifted_word(B.V + ob, B.n, A.n, r);
+            O.S[oo] = shifted_word(A.S + oa, A.n, 0, r) | shifted_word(B.S + ob, B.n, A.n, r);
+            O.GL[oo] = shifted_word(A.GL + oa, A.n, 0, r) | shifted_word(B.GL + ob, B.n, A.n, r);
+            O.GH[oo] = shifted_word(A.GH + oa, A.n, 0, r) | shifted_word(B.GH + ob, B.n, A.n, r);
+        }
+        if (r == 0) {
+            O.phase[term] = (uint8_t)((A.phase[i] + B.phase[j]) & 7);
+            O.coef_k[term] = (uint8_t)((A.coef_k[i] + B.coef_k[j]) & 7);
+            O.coef_r[term] = A.coef_r[i] + B.coef_r[j];
+        }
+    }
+}
+
+cudaError_t launch_kron(TermsView A, TermsView B, TermsView O, cudaStream_t st) {
+    if (O.chi == 0) return cudaSuccess;
+    const int64_t total = O.chi * O.R;
+    const int blocks = (int)std::min<int64_t>((total + 255) / 256, 65535);
+    kron_kernel<<<blocks, 256, 0, st>>>(A, B, O);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_statevector(const TermsView& t, double gf_re, double gf_im, double* out, cudaStream_t st) {
     int64_t dim = (int64_t)1 << t.n;
     int blocks = (int)std::min<int64_t>((dim + 255) / 256, 65535);

@@ -95,6 +95,13 @@ class QuantumState:
         check(_ffi.load().nsg_state_clone(self._h, C.byref(h)))
         return QuantumState(h)
 
+    def kron(self, other: "QuantumState") -> "QuantumState":
+        """|self⟩ ⊗ |other⟩ (other's qubits after self's), computed on the device term by term
+        (StabilizerDecomposedState::kron, stabilizer_decomposed_state/kron.rs:7-22)."""
+        h = C.c_void_p()
+        check(_ffi.load().nsg_state_kron(self._h, other._h, C.byref(h)))
+        return QuantumState(h)
+
     def set_stream(self, cuda_stream: int | None) -> None:
         """Run this state's work on a caller-owned cudaStream_t (an integer handle)."""
         check(_ffi.load().nsg_state_set_stream(self._h, C.c_void_p(cuda_stream or 0)))

@@ -315,3 +315,44 @@ def test_tiny_states_every_pauli(gpu_pkg, oracle, n, nc, nt, seed):
     _, amp_ex = rz.inner_product(ref)
     assert abs(amp - amp_ex) <= TOL
     assert np.allclose(st.to_statevector(), ref.to_statevector(), atol=1e-12)
+
+
+@pytest.mark.parametrize("na,nb,seed", [(1, 1, 81), (3, 5, 82), (20, 12, 83), (30, 34, 84), (40, 24, 85),
+                                        (64, 64, 86)])
+def test_state_kron_bit_exact(gpu_pkg, oracle, na, nb, seed):
+    """A ⊗ B on the device (stabilizer_decomposed_state/kron.rs:7-22): every term equal
+    to the oracle's, in i-major order; ⟨P_A ⊗ P_B⟩ = ⟨P_A⟩·⟨P_B⟩."""
+    ga = random_full_circuit(na, 12 * na, 3, seed)
+    gb = random_full_circuit(nb, 12 * nb, 2, seed + 100)
+    a = gpu_pkg.QuantumState.from_gates(na, ga)
+    b = gpu_pkg.QuantumState.from_gates(nb, gb)
+    k = a.kron(b)
+    assert k.num_qubits == na + nb and k.stabilizer_rank == a.stabilizer_rank * b.stabilizer_rank
+    rk = oracle.OracleState.from_circuit(na, ga).kron(oracle.OracleState.from_circuit(nb, gb))
+    assert_same_terms(k.export_terms(), rk.export_terms())
+    if na + nb <= 64:
+        rng = np.random.default_rng(seed)
+        for _ in range(3):
+            pa, pb = rng.integers(0, 4, na), rng.integers(0, 4, nb)
+            P = gpu_pkg.PauliString.dense
+            want = a.exp_value(P(pa)) * b.exp_value(P(pb))
+            assert close(k.exp_value(P(np.concatenate([pa, pb]))), want)
+    if na + nb <= 10:
+        assert np.abs(k.to_statevector() - np.kron(b.to_statevector(), a.to_statevector())).max() < 1e-9
+    k.apply_h(na + nb - 1)  # the product is an ordinary state
+    assert close(k.norm(), 1.0)
+
+
+def test_state_kron_global_factors(gpu_pkg):
+    ga, gb = toffoli_gates(), random_full_circuit(2, 20, 2, 87)
+    a = gpu_pkg.QuantumState.from_gates(3, ga)
+    b = gpu_pkg.QuantumState.from_gates(2, gb)
+    a.project_normalized(0, True)  # global factor ≠ 1
+    b.project_unnormalized(1, False)
+    k = a.kron(b)
+    assert np.abs(k.to_statevector() - np.kron(b.to_statevector(), a.to_statevector())).max() < 1e-9
+    e = gpu_pkg.QuantumState.from_gates(1, []).kron(a)
+    assert np.abs(e.to_statevector() - np.kron(a.to_statevector(), [1, 0])).max() < 1e-9
+    with pytest.raises(gpu_pkg.NecstarError) as err:
+        gpu_pkg.QuantumState.from_gates(100, []).kron(gpu_pkg.QuantumState.from_gates(29, []))
+    assert err.value.code == 105
