@@ -4,12 +4,12 @@
 // (mutekichi/stab-decomp-simulator-rust), one `bool` byte per tableau bit
 // exactly as the reference stores it (ndarray::Array2<bool>,
 // crates/stabilizer-ch-form-rust/src/form/mod.rs:12-22), with the same rule
-// order, pivot choices and term order.  It is the checker for the CUDA path:
+// order, pivot choices and term order.  The CUDA path is checked against it:
 // only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
 // it.  The product library never links or calls it.
 //
-// The reference is Rust and cannot be compiled in this environment (no
-// cargo/rustc), so this is a port.  Its outputs are pinned against the
+// The reference is Rust and no Rust toolchain was available to build it
+// (no cargo/rustc), so this is a port.  Its outputs are pinned against the
 // reference's own known-answer tests (T-tensor statevectors t=1..11, the
 // Toffoli-state expectation values, the χ=2 statevector, the doctest
 // amplitudes, the gate-API error variants) and against an independent dense

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle — TEST INFRASTRUCTURE ONLY.
 
 Used by ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
-``bench.py`` as the checker.  The product package never imports this module.
+``bench.py`` to check and time against.  The product package never imports this module.
 Gate lists are numpy ``uint32`` arrays of shape (N, 4) = (op, q0, q1, q2) with
 the opcodes of ``include/necstar_gpu.h``; Pauli strings are
 ``(kind, ops, qubits)`` triples (kind 0 dense little-endian, 1 sparse).
