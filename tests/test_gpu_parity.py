@@ -357,3 +357,33 @@ def test_state_kron_global_factors(gpu_pkg):
     with pytest.raises(gpu_pkg.NecstarError) as err:
         gpu_pkg.QuantumState.from_gates(100, []).kron(gpu_pkg.QuantumState.from_gates(29, []))
     assert err.value.code == 105
+
+
+@pytest.mark.parametrize("n", [1, 5, 20, 40, 64])
+def test_random_clifford_states_bit_exact(gpu_pkg, oracle, n):
+    """QuantumCircuit.random_clifford followed by T gates, compiled on the device:
+    terms equal the oracle's; ⟨P⟩ agrees with the oracle's exact value."""
+    c = gpu_pkg.QuantumCircuit.random_clifford(n, seed=1000 + n)
+    rng = np.random.default_rng(n)
+    for q in rng.integers(0, n, 4):
+        c.apply_t(int(q))
+    c.append(gpu_pkg.QuantumCircuit.random_clifford(n, seed=2000 + n))
+    st = gpu_pkg.QuantumState.from_circuit(c)
+    ref = oracle.OracleState.from_circuit(n, c.gate_array())
+    assert_same_terms(st.export_terms(), ref.export_terms())
+    ops = rng.integers(0, 4, n)
+    _, want = ref.exp_value(0, ops)
+    assert close(st.exp_value(gpu_pkg.PauliString.dense(ops)), want)
+
+
+def test_qasm_circuit_known_answer(gpu_pkg):
+    # the Toffoli-state circuit of tests/test_state_calculation.py:37-65 read from OpenQASM: ⟨ZII⟩ = 0.5
+    text = "\n".join(["OPENQASM 2.0;", 'include "qelib1.inc";', "qreg q[3];", "h q[0];", "h q[1];", "h q[2];",
+                      "cx q[1], q[2];", "tdg q[2];", "cx q[0], q[2];", "t q[2];", "cx q[1], q[2];", "tdg q[2];",
+                      "cx q[0], q[2];", "t q[1];", "t q[2];", "cx q[0], q[1];", "h q[2];", "t q[0];", "tdg q[1];",
+                      "cx q[0], q[1];", "measure q[0] -> c[0];"])
+    c = gpu_pkg.QuantumCircuit.from_qasm_str(text)
+    assert np.array_equal(c.gate_array(), toffoli_gates())
+    st = gpu_pkg.QuantumState.from_circuit(c)
+    assert close(st.exp_value(gpu_pkg.PauliString.from_str("ZII")), 0.5)
+    assert close(st.norm(), 1.0)
