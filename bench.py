@@ -323,6 +323,7 @@ def run_ours(args):
                        "l2": "flushed (256 MiB write) before every timed step", "parallelism": f"replicas x{ws}"},
             "inner_products_per_s": value * pairs,
             "path": "BatchPlan.run (nsg_plan_run: CUDA-graph replay), FP64",
+            "plan_tiling": plan.tiling,
             "direct": {"value": ws * nobs / (direct_ms * 1e-3), "unit": UNIT, "ms_per_step": direct_ms,
                        "path": "nsg_exp_value_batch"},
             "mixed": {"value": ws * nobs / (mixed_ms * 1e-3), "unit": UNIT,
