@@ -763,21 +763,27 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                 // 2·δ(hb = 0)), IO those with odd L (a factor √2·ω^{1-2hb}).
                 Word IE = 0, IO = 0;
                 while (alive) {
-                    // isolated variables (no coupling to another alive one) factor out
-                    Word iso = 0;
-#pragma unroll
-                    for (int k = 0; k < RPL; k++)
-                        iso |= (Word)__ballot_sync(FULL, (alive & own[k]) && !(J[k] & alive & ~own[k])) << (32 * k);
-                    IE |= iso & ~L0;
-                    IO |= iso & L0;
-                    alive &= ~iso;
-                    if (!alive) break;
-                    // then one coupled variable, with even L if there is one (an even
-                    // step removes two variables, which leaves fewer steps in all)
+                    // the next variable, with even L if there is one (an even step
+                    // removes two variables, which leaves fewer steps in all)
                     const Word even = alive & ~L0;
                     const int jq = ffs0<Word>(even ? even : alive);
                     const Word jb = (Word)1 << jq;
                     const Word S = row_of<Word, RPL>(J, jq) & alive & ~jb;
+                    if (!S) {
+                        // it is isolated (coupled to no other alive variable): all
+                        // isolated variables factor out together, found by one ballot.
+                        // An elimination never touches an isolated variable (its row
+                        // and column are zero among the alive ones), so they can wait
+                        // until a pivot is one of them.
+                        Word iso = 0;
+#pragma unroll
+                        for (int k = 0; k < RPL; k++)
+                            iso |= (Word)__ballot_sync(FULL, (alive & own[k]) && !(J[k] & alive & ~own[k])) << (32 * k);
+                        IE |= iso & ~L0;
+                        IO |= iso & L0;
+                        alive &= ~iso;
+                        continue;
+                    }
                     alive &= ~jb;
                     if ((L0 >> jq) & 1) {  // 1 + i^{L_j}(-1)^{S·z} = √2·ω^{±1}·i^{∓S·z}
                         IO |= jb;
