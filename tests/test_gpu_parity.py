@@ -64,6 +64,36 @@ def test_small_benchmark_circuit_bit_exact(gpu_pkg, oracle):
     assert_same_terms(st.export_terms(), ref.export_terms())
 
 
+def test_small_benchmark_outputs(gpu_pkg, oracle):
+    """The outputs asked of the n = 16 workload: ⟨Z₀⟩; the amplitude ⟨0¹⁶|ψ⟩, which the reference
+    obtains as from_circuit(QuantumCircuit::new(16)).inner_product(ψ) (state/mod.rs:165-172);
+    and sample(0..15, 1024), whose bit-0 frequency and total parity follow ⟨Z₀⟩ and ⟨Z^{⊗16}⟩."""
+    cfg = W.SMALL_N16
+    n = cfg["n"]
+    g = W.random_clifford_t_circuit(n, cfg["num_clifford"], cfg["num_t"], cfg["seed"])
+    st = gpu_pkg.QuantumState.from_gates(n, g)
+    ref = oracle.OracleState.from_circuit(n, g)
+    z0 = [3] + [0] * (n - 1)
+    _, want_z0 = ref.exp_value(0, z0)
+    got_z0 = st.exp_value(gpu_pkg.PauliString.dense(z0))
+    assert close(got_z0, want_z0)
+    empty = np.zeros((0, 4), np.uint32)
+    amp = gpu_pkg.QuantumState.from_gates(n, empty).inner_product(st)
+    _, want_amp = oracle.OracleState.from_circuit(n, empty).inner_product(ref)
+    assert abs(amp - want_amp) <= TOL
+    assert abs(amp - st.to_statevector()[0]) <= TOL
+    shots = 1024
+    vals, cnts = st.sample_raw(list(range(n)), shots, seed=16)
+    assert sum(cnts) == shots
+    probs = np.abs(st.to_statevector()) ** 2
+    assert all(probs[v] > 1e-12 for v in vals)
+    zall = st.exp_value(gpu_pkg.PauliString.dense([3] * n))
+    f0 = sum(c for v, c in zip(vals, cnts) if not v & 1) / shots
+    fpar = sum(c for v, c in zip(vals, cnts) if bin(v).count("1") % 2 == 0) / shots
+    assert abs(f0 - (1 + got_z0) / 2) < 5 * 0.5 / shots ** 0.5
+    assert abs(fpar - (1 + zall) / 2) < 5 * 0.5 / shots ** 0.5
+
+
 @pytest.mark.parametrize("t", [1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 13, 16, 21, 24])
 def test_device_t_tensor_bit_exact(gpu_pkg, oracle, t):
     """The device expansion of |T⟩^{⊗t} (t_state.rs:29-71): every term, phase and
