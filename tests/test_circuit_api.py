@@ -304,3 +304,23 @@ def test_random_clifford_uniform_two_qubit_states(nec):
         counts[key] = counts.get(key, 0) + 1
     assert len(counts) == 60  # every two-qubit stabilizer state
     assert _chi2_ok(counts, 60, samples)
+
+
+def test_random_clifford_abi_arguments(nec):
+    """nsg_random_clifford / nsg_random_words argument handling (no device work)."""
+    from stab_decomp_simulator_rust_gb300 import _ffi
+    L = _ffi.load()
+    consts = _ffi.header_constants()
+    nout = C.c_size_t(7)
+    assert L.nsg_random_clifford(3, None, None, 0, None) == consts["NSG_ERR_INVALID_ARGUMENT"]
+    assert L.nsg_random_clifford(0, None, None, 0, C.byref(nout)) == 0 and nout.value == 0
+    small = (C.c_uint32 * 16)()
+    assert L.nsg_random_clifford(3, bytes(32), small, 4, C.byref(nout)) == consts["NSG_ERR_BUFFER_TOO_SMALL"]
+    args = (C.c_int64 * 3)()
+    L.nsg_last_error_args(args)
+    assert list(args)[:2] == [2 * 9 + 9, 4]
+    assert L.nsg_random_words(None, small, 4) == consts["NSG_ERR_INVALID_ARGUMENT"]
+    assert L.nsg_random_words(bytes(32), None, 0) == 0
+    inp = (C.c_uint32 * 16)()
+    for bad in (0, 3, -2, 66):
+        assert L.nsg_debug_chacha_block(inp, bad, small) == consts["NSG_ERR_INVALID_ARGUMENT"]
