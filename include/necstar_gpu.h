@@ -298,7 +298,7 @@ nsg_status nsg_state_kron(const nsg_state* a, const nsg_state* b, nsg_state** ou
  * form U = F1·H·S·F2, drawn and emitted in the reference's order from the
  * seeded stream below).  out must hold 2n² + 3n gates (the bound; fewer are
  * written, *num_out of them); seed32 may be NULL (entropy); n = 0 gives no
- * gates. */
+ * gates; n ≤ 2^24. */
 nsg_status nsg_random_clifford(uint32_t n, const uint8_t* seed32, nsg_gate* out, size_t capacity,
                                size_t* num_out);
 

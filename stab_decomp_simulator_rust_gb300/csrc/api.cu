@@ -2091,6 +2091,8 @@ nsg_status nsg_random_clifford(uint32_t n, const uint8_t* seed32, nsg_gate* out,
     API_BEGIN
     need(num_out, "num_out");
     *num_out = 0;
+    if (n > (1u << 24))  // 2n² + 3n gates and n² bytes per layer matrix must stay addressable
+        raise(NSG_ERR_INVALID_ARGUMENT, n, 1 << 24, "random Clifford circuits are limited to 2^24 qubits, got %u", n);
     const uint64_t bound = random_clifford_max_gates(n);
     if (bound) need(out, "out");
     if (capacity < bound)
