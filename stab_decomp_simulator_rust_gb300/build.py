@@ -19,7 +19,7 @@ CSRC = os.path.join(PKG, "csrc")
 OUT_DIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(OUT_DIR, "libnecstar_gpu.so")
 SOURCES = ["api.cu", "kernels_terms.cu", "kernels_pairs.cu", "noalloc.cu"]
-HEADERS = ["warp_chform.cuh", "device_state.hpp", "chform_host.hpp", "host_rng.hpp"]
+HEADERS = ["warp_chform.cuh", "device_state.hpp", "chform_host.hpp", "host_rng.hpp", "random_clifford.hpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
