@@ -231,3 +231,17 @@ def test_reference_order_fp64_close_to_exact(oracle):
         p = rng.integers(0, 4, 8)
         ref, ex = st.exp_value(0, p)
         assert abs(ref - ex) < 1e-12
+
+
+@pytest.mark.parametrize("seed", [61, 62, 63])
+def test_kron_vs_statevectors(oracle, seed):
+    # stabilizer_decomposed_state/kron.rs:27-45: the kron state's statevector is the
+    # tensor product of the factors' (qubits of the second factor after the first's)
+    ga = random_full_circuit(3, 40, 3, seed)
+    gb = random_full_circuit(4, 50, 2, seed + 10)
+    a = oracle.OracleState.from_circuit(3, ga)
+    b = oracle.OracleState.from_circuit(4, gb)
+    k = a.kron(b)
+    assert k.num_qubits == 7 and k.stabilizer_rank == a.stabilizer_rank * b.stabilizer_rank
+    assert np.abs(k.to_statevector() - np.kron(b.to_statevector(), a.to_statevector())).max() < 1e-9
+    assert np.abs(k.to_statevector() - np.kron(oracle.dense_simulate(4, gb), oracle.dense_simulate(3, ga))).max() < 1e-9
