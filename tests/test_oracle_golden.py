@@ -245,3 +245,15 @@ def test_kron_vs_statevectors(oracle, seed):
     assert k.num_qubits == 7 and k.stabilizer_rank == a.stabilizer_rank * b.stabilizer_rank
     assert np.abs(k.to_statevector() - np.kron(b.to_statevector(), a.to_statevector())).max() < 1e-9
     assert np.abs(k.to_statevector() - np.kron(oracle.dense_simulate(4, gb), oracle.dense_simulate(3, ga))).max() < 1e-9
+
+
+def test_measure_uses_the_seeded_stream(oracle):
+    # measurement.rs:34-103: one rng.gen::<f64>() per measured qubit, outcome 1 iff the draw is not
+    # below p0/(p0+p1); on |+⟩^n every p0 is 1/2, so the outcomes are the stream's.
+    n = 10
+    plus = g(*[(H, q) for q in range(n)])
+    for s in range(5):
+        seed = bytes([3 * s + 2]) * 32
+        st = oracle.OracleState.from_circuit(n, plus)
+        u = oracle.random_doubles(seed, n)
+        assert st.measure(list(range(n)), seed) == [bool(x >= 0.5) for x in u]
