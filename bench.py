@@ -331,7 +331,8 @@ def run_ours(args):
             "plain": {"value": plain_rate * ws, "unit": UNIT, "path": "nsg_exp_value, one observable per call"},
             "e2e": e2e, "roofline": roofline, "clocks": clocks.summary(), "gpu_launches": None}
     # kernels launched per timed step (one plan replay): frames, term tables, Pauli frames, pairs, reduction
-    line["gpu_launches"] = 5 * args.steps
+    # per replay: frames, term tables, Pauli frames, the pair launch and the two reduction passes
+    line["gpu_launches"] = 6 * args.steps
     if rank == 0:
         if not args.no_cpu:
             try:
@@ -413,7 +414,8 @@ def run_precision60(args, torch, L):
             "plain": {"value": 1.0 / (ms1 * 1e-3), "unit": UNIT, "path": "nsg_exp_value, one observable per call"},
             "mixed_rel_err_vs_fp64": {"max": float(err.max()), "median": float(np.median(err)),
                                       "per_observable": [float(x) for x in err]},
-            "clocks": clocks.summary(), "gpu_launches": 3 * args.steps}
+            # per call: Pauli frames, the pair launch, the two reduction passes (frames and tables are cached)
+            "clocks": clocks.summary(), "gpu_launches": 4 * args.steps}
     print(json.dumps(line))
 
 
@@ -493,7 +495,10 @@ def run_batch512(args, torch, L):
                     "h2d_bytes_per_step": int(sum(g.nbytes for g in pinned) + sum(p.ops.nbytes for ps in plists for p in ps)),
                     "d2h_bytes_per_step": int(8 * nobs),
                     "path": "nsg_state_from_circuit x512 + nsg_exp_value_multi, host buffers"},
-            "clocks": clocks.summary()}
+            "clocks": clocks.summary(),
+            # per replay: frames and term tables per state, Pauli frames per state, and per row width
+            # (32- and 64-bit) one pair launch and two reduction passes
+            "gpu_launches": args.steps * (3 * len(states) + 3 * len({n <= 32 for (n, _, _) in circuits}))}
     print(json.dumps(line))
 
 
