@@ -5,8 +5,8 @@
  * `QuantumState` API (crates/necstar/src/state/mod.rs:67-706).  Every call
  * returns an `nsg_status`; results go into caller-provided buffers; a state is
  * an opaque handle that owns its χ CH-form terms in device memory.  A Rust
- * crate binds these with `extern "C"`, Python binds them
- * with ctypes (stab_decomp_simulator_rust_gb300/_ffi.py).
+ * crate binds these with `extern "C"` declarations of the same signatures;
+ * Python binds them with ctypes (stab_decomp_simulator_rust_gb300/_ffi.py).
  *
  * Threading: each state owns one CUDA stream.  Calls on different states may
  * run concurrently from different host threads; calls on the same state must be
@@ -115,6 +115,12 @@ enum nsg_precision {
                                 power-of-two scaling, FP64 final reduction  */
 };
 
+/* Exact accumulation (nsg_exp_value_counts): every pair term of the χ² sum
+ * has a real part sign·2^(-m/2) for an integer m; the count for m is at
+ * index m + NSG_EXACT_M_OFFSET of NSG_EXACT_BINS bins.                       */
+#define NSG_EXACT_BINS                       512
+#define NSG_EXACT_M_OFFSET                   192
+
 typedef struct nsg_state nsg_state;
 
 /* ------------------------------------------------------------------------ */
@@ -139,6 +145,16 @@ nsg_status nsg_last_error_args(int64_t out[3]);
  * (crates/necstar/src/state/mod.rs:98-102 → state/compiler/mod.rs:44-140). */
 nsg_status nsg_state_from_circuit(uint32_t num_qubits, const nsg_gate* gates,
                                   size_t num_gates, nsg_state** out);
+
+/* Batched form of nsg_state_from_circuit (no reference counterpart): circuit
+ * c (num_qubits[c], gates[c][0..num_gates[c])) becomes out[c], the same
+ * state nsg_state_from_circuit gives.  Every circuit is validated and its
+ * compile queued on its own stream before the call waits for any of them.
+ * On an error no state is returned and the failing circuit's index is in
+ * nsg_last_error_args()[2]. */
+nsg_status nsg_states_from_circuits(size_t num_circuits, const uint32_t* num_qubits,
+                                    const nsg_gate* const* gates, const size_t* num_gates,
+                                    nsg_state** out);
 
 /* Builds a state from explicit CH-form terms given as bool bytes (the layout
  * of nsg_export_terms).  Replaces StabilizerDecomposedState::new
@@ -196,16 +212,38 @@ nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states
                                const nsg_pauli* paulis, const uint64_t* pauli_offsets,
                                uint32_t precision, double* out);
 
+/* The exact accumulator of exp_value (no reference counterpart; the exact sum
+ * the FP64 and mixed results are measured against): for observable o,
+ * counts[o·NSG_EXACT_BINS + m + NSG_EXACT_M_OFFSET] is the signed number of
+ * pair terms of the reference's χ² sum (stabilizer_decomposed_state/
+ * exp_value.rs:38-58, the j > i terms counted twice) whose real part is
+ * 2^(-m/2), so ⟨P_o⟩ = scale·Σ_m counts[..m..]·2^(-m/2) exactly, with
+ * *scale = |global factor|² (may be NULL).  Integer counts: the result does
+ * not depend on the schedule.  An exponent outside the bins gives
+ * NSG_ERR_INVALID_ARGUMENT. */
+nsg_status nsg_exp_value_counts(const nsg_state* state, const nsg_pauli* paulis, size_t num_paulis,
+                                int64_t* counts, double* scale);
+
+/* Tiling of the direct (uncaptured) pair sums of this process: kets per
+ * chunk and tasks per resident warp of the persistent pair launch; 0 keeps
+ * the default (32 and 8).  Results do not depend on it beyond FP rounding
+ * of the partial sums (no reference counterpart). */
+nsg_status nsg_set_pair_tiling(int32_t chunk, int32_t tasks_per_warp);
+
 /* ⟨P⟩ for callers that cannot allocate device memory at call time — a
  * process whose GPU memory is already fully reserved by another allocator,
  * or a latency-critical loop where cudaMalloc/cudaFree would synchronise the
  * device.  Same value as nsg_exp_value; no counterpart in the reference.
  * All scratch comes from one 16 MiB static device array (held by every GPU
- * that loads the library until exit): n ≤ 64 and χ ≤ 8192, larger states give
- * NSG_ERR_BUFFER_TOO_SMALL.  The first call on a device looks up the array's
- * address (make it before any stream capture); all calls share the array,
- * so calls that overlap on the GPU race.  Synchronous: *out is a host
- * double. */
+ * that loads the library until exit): n ≤ 64 (NSG_ERR_TOO_WIDE above) and
+ * χ ≤ 8192 (NSG_ERR_BUFFER_TOO_SMALL above).  The first call on a device
+ * looks up the array's address (make it before any stream capture); CUDA
+ * loads device code lazily, so the array's memory is taken when that first
+ * call runs: make one call on each device before another allocator reserves
+ * its memory (or set CUDA_MODULE_LOADING=EAGER).  Like every entry point the
+ * call runs on the state's device and restores the caller's.  All calls
+ * share the array, so calls that overlap on the GPU race.  Synchronous: *out
+ * is a host double. */
 nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pauli* pauli, double* out);
 
 /* A captured batched evaluation (no reference counterpart): the work of
@@ -351,6 +389,28 @@ nsg_status nsg_probe_int_ops(uint64_t iters, double* seconds, uint64_t* ops);
  * full χ×χ square with the production pair kernel; for parity tests. */
 nsg_status nsg_debug_pair_values(const nsg_state* state, const nsg_pauli* pauli,
                                  uint8_t* k, int32_t* r);
+
+/* Diagnostic: compiles the circuit like nsg_state_from_circuit and writes,
+ * per term of |T⟩^{⊗t} (in the expansion's order), keep = 1 when the term
+ * survives the post-selection of the ancillas (compiler/mod.rs:108-131);
+ * the compiled state's term i is the i-th kept term.  *num_t_terms is the
+ * expansion's size (NSG_ERR_BUFFER_TOO_SMALL above capacity). */
+nsg_status nsg_debug_compile_keep(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates,
+                                  uint8_t* keep, size_t capacity, uint64_t* num_t_terms);
+
+/* A new state holding the terms indices[0..count) (strictly ascending) of
+ * `state`, with their coefficients and the same global factor; for sampled
+ * parity checks of large states (no reference counterpart). */
+nsg_status nsg_state_select(const nsg_state* state, const uint64_t* indices, size_t count, nsg_state** out);
+
+/* Test hook for the bounded barrier waits of the pair kernel (the waits that
+ * replace a hang by NSG_ERR_TIMEOUT): poll_limit polls per wait (0 restores
+ * 2^22) and, when extra_tx_bytes > 0 (≤ 1024), the barrier of the first ket
+ * of every chunk expects that many bytes more than its bulk copy delivers,
+ * so that wait runs out after the copy has landed and the call returns
+ * NSG_ERR_TIMEOUT with no copy in flight.  Applies to launches built after
+ * the call; 0, 0 restores normal operation. */
+nsg_status nsg_debug_set_wait(uint32_t poll_limit, uint32_t extra_tx_bytes);
 
 /* The device expansion of |T⟩^{⊗t} (construct_t_tensor_state,
  * crates/necstar/src/state/magic_states/t_state.rs:29-71; 1 ≤ t ≤ 64) as a

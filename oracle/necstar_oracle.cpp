@@ -870,11 +870,50 @@ static SDState construct_t_tensor(int nq) {
     return r;
 }
 
+// One term of construct_cat(nq) (cat_state.rs:162-188) without building the
+// others.  The recursion's term order is i-major over kron(cat(nq-4), cat(6))
+// (stabilizer_decomposed_state/kron.rs:11-16) and every later step
+// (project_onto_cat, reduce_cat) acts on each term alone, so term ci is
+// term ci/3 of cat(nq-4) joined with term ci%3 of cat(6).
+static int64_t cat_rank(int nq) {
+    static const int64_t small[7] = {0, 1, 1, 2, 2, 3, 3};
+    if (nq <= 0) fail(NSG_ERR_INVALID_NUM_QUBITS, 0);
+    return nq <= 6 ? small[nq] : cat_rank(nq - 4) * 3;
+}
+static std::pair<ChForm, Scalar> cat_term(int nq, int64_t ci) {
+    if (ci < 0 || ci >= cat_rank(nq)) fail(NSG_ERR_QUBIT_INDEX_OUT_OF_BOUNDS, ci, cat_rank(nq));
+    if (nq <= 6) {
+        SDState s = construct_cat(nq);
+        return {s.stabs[(size_t)ci], s.coeffs[(size_t)ci]};
+    }
+    auto a = cat_term(nq - 4, ci / 3);
+    SDState c6 = cat6();
+    ChForm st = kron(a.first, c6.stabs[(size_t)(ci % 3)]);
+    project_onto_cat(st, nq - 5, nq - 4);
+    return {st, scalar_mul(a.second, c6.coeffs[(size_t)(ci % 3)])};
+}
+// Term k of construct_t_tensor(nq) (t_state.rs:29-71): cat terms first
+// (coefficient·2^(-1/2)), then their copies with X·S on qubit 0 (·e^(-iπ/4)).
+static int64_t t_tensor_rank(int nq) { return 2 * cat_rank(nq); }
+static std::pair<ChForm, Scalar> t_tensor_term(int nq, int64_t k) {
+    const int64_t cr = cat_rank(nq);
+    if (k < 0 || k >= 2 * cr) fail(NSG_ERR_QUBIT_INDEX_OUT_OF_BOUNDS, k, 2 * cr);
+    auto c = cat_term(nq, k % cr);
+    Scalar coef = scalar_mul(c.second, S_ONE_OVER_SQRT2);
+    if (k >= cr) {
+        left_x(c.first, 0);
+        left_s(c.first, 0);
+        coef = scalar_mul(coef, Scalar{false, 7, 0});
+    }
+    return {c.first, coef};
+}
+
 // ---------------------------------------------------------------------------
 // Compiler (crates/necstar/src/state/compiler/mod.rs:44-140)
 static bool is_clifford_op(uint32_t op) { return op <= NSG_GATE_SWAP; }
 
-static SDState compile(int n, const std::vector<nsg_gate>& gates) {
+// Lowering (compiler/mod.rs:49-63): T/Tdg -> CX(target, n+k) [+ Sdg(target)].
+static std::vector<nsg_gate> lower_circuit(int n, const std::vector<nsg_gate>& gates, int* t_out) {
     int t = 0;
     std::vector<nsg_gate> cl;
     for (const auto& g : gates) {
@@ -889,6 +928,35 @@ static SDState compile(int n, const std::vector<nsg_gate>& gates) {
             fail(NSG_ERR_GATE_NOT_SUPPORTED, g.op, -1, "Gate CCX is not supported.");
         }
     }
+    *t_out = t;
+    return cl;
+}
+
+// The per-term body of the compile loop (compiler/mod.rs:92-131): kron with
+// |0^n⟩, every Clifford, post-selection of the ancillas in reverse order;
+// false when a projection is impossible (the term is dropped).
+static bool compile_one(int n, int t, const std::vector<nsg_gate>& cl, const ChForm& tterm, Scalar tcoef,
+                        ChForm& out, Scalar& coef) {
+    ChForm full = kron(ch_new(n), tterm);
+    for (const auto& g : cl) apply_clifford(full, g);
+    int ndet = 0;
+    for (int q = n + t - 1; q >= n; q--) {
+        try {
+            if (project(full, q, false)) ndet++;
+        } catch (const Error& e) {
+            if (e.code == NSG_ERR_IMPOSSIBLE_PROJECTION) return false;
+            throw;
+        }
+    }
+    for (int q = n + t - 1; q >= n; q--) discard(full, q);
+    out = std::move(full);
+    coef = scalar_amplify(tcoef, ndet);
+    return true;
+}
+
+static SDState compile(int n, const std::vector<nsg_gate>& gates) {
+    int t = 0;
+    std::vector<nsg_gate> cl = lower_circuit(n, gates, &t);
     if (t == 0) {  // :66-80
         ChForm c = ch_new(n);
         for (const auto& g : cl) apply_clifford(c, g);
@@ -898,22 +966,65 @@ static SDState compile(int n, const std::vector<nsg_gate>& gates) {
     SDState out;
     out.num_qubits = n;
     for (size_t k = 0; k < tt.stabs.size(); k++) {
-        ChForm full = kron(ch_new(n), tt.stabs[k]);
-        for (const auto& g : cl) apply_clifford(full, g);
-        bool ok = true;
-        int ndet = 0;
-        for (int q = n + t - 1; q >= n; q--) {
-            try {
-                if (project(full, q, false)) ndet++;
-            } catch (const Error& e) {
-                if (e.code == NSG_ERR_IMPOSSIBLE_PROJECTION) { ok = false; break; }
-                throw;
-            }
-        }
-        if (ok) {
-            for (int q = n + t - 1; q >= n; q--) discard(full, q);
+        ChForm full;
+        Scalar coef;
+        if (compile_one(n, t, cl, tt.stabs[k], tt.coeffs[k], full, coef)) {
             out.stabs.push_back(std::move(full));
-            out.coeffs.push_back(scalar_amplify(tt.coeffs[k], ndet));
+            out.coeffs.push_back(coef);
+        }
+    }
+    return out;
+}
+
+// The compile loop restricted to the T-tensor terms `tidx` (each built on its
+// own by t_tensor_term): the kept terms in the order given, kept[i] = 1 when
+// term tidx[i] survives post-selection.  Terms are independent in the loop
+// and the drop rule depends on the term alone, so these are exactly the
+// terms the whole compile keeps for those indices.
+static SDState compile_terms(int n, const std::vector<nsg_gate>& gates, const std::vector<int64_t>& tidx,
+                             uint8_t* kept, int threads) {
+    int t = 0;
+    std::vector<nsg_gate> cl = lower_circuit(n, gates, &t);
+    SDState out;
+    out.num_qubits = n;
+    if (t == 0) {
+        for (size_t i = 0; i < tidx.size(); i++) {
+            if (tidx[i] != 0) fail(NSG_ERR_QUBIT_INDEX_OUT_OF_BOUNDS, tidx[i], 1);
+            ChForm c = ch_new(n);
+            for (const auto& g : cl) apply_clifford(c, g);
+            out.stabs.push_back(c);
+            out.coeffs.push_back(S_ONE);
+            kept[i] = 1;
+        }
+        return out;
+    }
+    const size_t m = tidx.size();
+    std::vector<ChForm> terms(m);
+    std::vector<Scalar> coefs(m);
+    std::vector<uint8_t> ok(m, 0);
+    std::vector<Error> errs;
+    std::mutex emu;
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (int th = 0; th < std::max(1, threads); th++)
+        pool.emplace_back([&]() {
+            try {
+                for (size_t i; (i = next.fetch_add(1)) < m;) {
+                    auto tt = t_tensor_term(t, tidx[i]);
+                    ok[i] = compile_one(n, t, cl, tt.first, tt.second, terms[i], coefs[i]) ? 1 : 0;
+                }
+            } catch (const Error& e) {
+                std::lock_guard<std::mutex> lk(emu);
+                errs.push_back(e);
+            }
+        });
+    for (auto& th : pool) th.join();
+    if (!errs.empty()) throw errs[0];
+    for (size_t i = 0; i < m; i++) {
+        kept[i] = ok[i];
+        if (ok[i]) {
+            out.stabs.push_back(std::move(terms[i]));
+            out.coeffs.push_back(coefs[i]);
         }
     }
     return out;
@@ -1067,6 +1178,77 @@ static double exp_value(const SDState& st, const Pauli& p, double* exact_out) {
     double gf2 = std::norm(st.global_factor);
     if (exact_out) *exact_out = ex.value() * gf2;
     return acc.real() * gf2;
+}
+
+// The exact accumulator of exp_value as integer counts: every term of the
+// χ² sum (exp_value.rs:38-58, with the factor 2 of the j > i terms) has a
+// real part sign·2^(-m/2); counts[o][m + m_off] is the signed number of
+// them for observable o, so ⟨P_o⟩ = |g|²·Σ_m counts[o][m+m_off]·2^(-m/2)
+// exactly.  Rows i are spread over `threads` host threads, each with its
+// own counts (integer sums: the result does not depend on the split).
+static void exp_value_counts(const SDState& st, const std::vector<Pauli>& ps, int threads, int64_t m_off,
+                             int64_t bins, int64_t* counts) {
+    for (const Pauli& p : ps) validate_pauli(st, p);
+    const size_t chi = st.stabs.size(), nobs = ps.size();
+    threads = std::max(1, threads);
+    std::vector<std::vector<int64_t>> part(threads, std::vector<int64_t>((size_t)(nobs * bins), 0));
+    std::atomic<size_t> next{0};
+    std::vector<Error> errs;
+    std::mutex emu;
+    std::vector<std::thread> pool;
+    for (int th = 0; th < threads; th++)
+        pool.emplace_back([&, th]() {
+            try {
+                int64_t* c = part[th].data();
+                auto add = [&](size_t o, Scalar tt, int64_t w) {
+                    if (tt.zero) return;
+                    int sgn;
+                    int64_t m;
+                    switch (tt.k & 7) {
+                        case 0: sgn = 1; m = tt.r; break;
+                        case 4: sgn = -1; m = tt.r; break;
+                        case 1: case 7: sgn = 1; m = tt.r + 1; break;
+                        case 3: case 5: sgn = -1; m = tt.r + 1; break;
+                        default: return;
+                    }
+                    if (m + m_off < 0 || m + m_off >= bins) fail(NSG_ERR_DEVICE_INVARIANT, m, bins, "exact count range");
+                    c[o * bins + (m + m_off)] += sgn * w;
+                };
+                for (size_t i; (i = next.fetch_add(1)) < chi;) {
+                    for (size_t o = 0; o < nobs; o++) {
+                        ChForm ev = st.stabs[i];
+                        apply_pauli(ev, ps[o]);
+                        add(o, scalar_mul(scalar_mul(scalar_conj(st.coeffs[i]), st.coeffs[i]),
+                                          ch_inner_product_scalar(st.stabs[i], ev)), 1);
+                        for (size_t j = i + 1; j < chi; j++)
+                            add(o, scalar_mul(scalar_mul(scalar_conj(st.coeffs[j]), st.coeffs[i]),
+                                              ch_inner_product_scalar(st.stabs[j], ev)), 2);
+                    }
+                }
+            } catch (const Error& e) {
+                std::lock_guard<std::mutex> lk(emu);
+                errs.push_back(e);
+            }
+        });
+    for (auto& th : pool) th.join();
+    if (!errs.empty()) throw errs[0];
+    std::fill(counts, counts + nobs * bins, 0);
+    for (int th = 0; th < threads; th++)
+        for (size_t x = 0; x < (size_t)(nobs * bins); x++) counts[x] += part[th][x];
+}
+
+// Σ_m counts[m + m_off]·2^(-m/2), evaluated exactly and rounded once.
+static double counts_value(const int64_t* counts, int64_t m_off, int64_t bins) {
+    ExactSum ex;
+    for (int64_t b = 0; b < bins; b++) {
+        const int64_t c = counts[b];
+        if (c == 0) continue;
+        const int64_t m = b - m_off;
+        const uint64_t mag = (uint64_t)(c < 0 ? -c : c);
+        if (((m % 2) + 2) % 2 == 0) (c > 0 ? ex.xp : ex.xn).add(mag, -(m / 2));
+        else (c > 0 ? ex.yp : ex.yn).add(mag, -((m - 1) / 2));
+    }
+    return ex.value();
 }
 
 // norm_squared (stabilizer_decomposed_state/norm.rs:8-30)
@@ -1508,6 +1690,57 @@ int orc_t_tensor_state(uint32_t t, void** out) {
 int orc_cat_state(uint32_t t, void** out) {
     ORC_TRY
     *out = new SDState(construct_cat((int)t));
+    ORC_CATCH
+}
+
+// Terms tidx[0..count) of the T-tensor state |T⟩^{⊗t}, each built on its own.
+int orc_t_tensor_terms(uint32_t t, const int64_t* tidx, size_t count, void** out) {
+    ORC_TRY
+    SDState* st = new SDState();
+    st->num_qubits = (int)t;
+    for (size_t i = 0; i < count; i++) {
+        auto tt = t_tensor_term((int)t, tidx[i]);
+        st->stabs.push_back(tt.first);
+        st->coeffs.push_back(tt.second);
+    }
+    *out = st;
+    ORC_CATCH
+}
+
+int orc_t_tensor_rank(uint32_t t, uint64_t* out) {
+    ORC_TRY
+    *out = t == 0 ? 1 : (uint64_t)t_tensor_rank((int)t);
+    ORC_CATCH
+}
+
+// The compile loop over the chosen T-tensor terms only (kept[i] per term).
+int orc_compile_terms(uint32_t n, const nsg_gate* gates, size_t ng, const int64_t* tidx, size_t count,
+                      int32_t threads, uint8_t* kept, void** out) {
+    ORC_TRY
+    std::vector<nsg_gate> gv(gates, gates + ng);
+    std::vector<int64_t> ti(tidx, tidx + count);
+    *out = new SDState(compile_terms((int)n, gv, ti, kept, threads));
+    ORC_CATCH
+}
+
+// Signed counts of the real parts of exp_value's pair terms per power of
+// √2 (counts[o·bins + m + m_off]), and each observable's exact value.
+int orc_exp_value_counts(void* stv, const nsg_pauli* ps, size_t nobs, int32_t threads, int64_t m_off, int64_t bins,
+                         int64_t* counts, double* exact) {
+    ORC_TRY
+    SDState* st = (SDState*)stv;
+    std::vector<Pauli> pv;
+    for (size_t o = 0; o < nobs; o++) pv.push_back(pauli_from_abi(&ps[o]));
+    exp_value_counts(*st, pv, threads, m_off, bins, counts);
+    const double gf2 = std::norm(st->global_factor);
+    for (size_t o = 0; o < nobs; o++) exact[o] = counts_value(counts + o * bins, m_off, bins) * gf2;
+    ORC_CATCH
+}
+
+// Σ_m counts[m + m_off]·2^(-m/2), exactly, rounded once (for counts from any source).
+int orc_counts_value(const int64_t* counts, int64_t m_off, int64_t bins, double* out) {
+    ORC_TRY
+    *out = counts_value(counts, m_off, bins);
     ORC_CATCH
 }
 

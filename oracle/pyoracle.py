@@ -75,6 +75,13 @@ def lib():
         L.orc_chform_run.argtypes = [C.c_uint32, C.c_void_p, C.c_size_t] + [C.c_void_p] * 8
         L.orc_time_pairs.argtypes = [vp, C.POINTER(PauliABI), C.c_uint64, C.c_uint64, C.c_int32,
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_t_tensor_terms.argtypes = [C.c_uint32, C.c_void_p, C.c_size_t, C.POINTER(vp)]
+        L.orc_t_tensor_rank.argtypes = [C.c_uint32, C.POINTER(C.c_uint64)]
+        L.orc_compile_terms.argtypes = [C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int32,
+                                        C.c_void_p, C.POINTER(vp)]
+        L.orc_exp_value_counts.argtypes = [vp, C.POINTER(PauliABI), C.c_size_t, C.c_int32, C.c_int64, C.c_int64,
+                                           C.c_void_p, C.c_void_p]
+        L.orc_counts_value.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.POINTER(C.c_double)]
         _lib = L
     return _lib
 
@@ -139,6 +146,27 @@ class OracleState:
         return OracleState(h)
 
     @staticmethod
+    def t_tensor_terms(t: int, tidx) -> "OracleState":
+        """Terms tidx of |T⟩^{⊗t}, each built on its own (the cat recursion for one term)."""
+        ti = np.ascontiguousarray(tidx, dtype=np.int64)
+        h = C.c_void_p()
+        _check(lib().orc_t_tensor_terms(t, _ptr(ti), len(ti), C.byref(h)))
+        return OracleState(h)
+
+    @staticmethod
+    def compile_terms(n: int, gates, tidx, threads: int = 0):
+        """The compile loop over the T-tensor terms `tidx` only (compiler/mod.rs:92-131).
+
+        Returns (state of the kept terms in tidx order, kept flags)."""
+        g = gates_array(gates)
+        ti = np.ascontiguousarray(tidx, dtype=np.int64)
+        kept = np.zeros(len(ti), np.uint8)
+        h = C.c_void_p()
+        _check(lib().orc_compile_terms(n, _ptr(g), len(g), _ptr(ti), len(ti), threads or (os.cpu_count() or 1),
+                                       _ptr(kept), C.byref(h)))
+        return OracleState(h), kept.astype(bool)
+
+    @staticmethod
     def from_terms(d: dict) -> "OracleState":
         n = int(d["n"])
         chi = int(len(d["phase"]))
@@ -196,6 +224,22 @@ class OracleState:
         out, ex = C.c_double(), C.c_double()
         _check(lib().orc_exp_value(self._h, C.byref(st), C.byref(out), C.byref(ex)))
         return out.value, ex.value
+
+    def exp_value_counts(self, paulis, m_off: int, bins: int, threads: int = 0):
+        """Exact accumulator of exp_value for several Paulis ((kind, ops, qubits) triples):
+        signed counts of pair-term real parts per power of √2 (shape (nobs, bins), index
+        m + m_off for sign·2^(-m/2)) and each exact value."""
+        abis, keep = [], []
+        for p in paulis:
+            st, k = pauli_abi(*p)
+            abis.append(st)
+            keep.append(k)
+        arr = (PauliABI * max(1, len(abis)))(*abis)
+        counts = np.zeros((len(abis), bins), np.int64)
+        exact = np.zeros(len(abis), np.float64)
+        _check(lib().orc_exp_value_counts(self._h, arr, len(abis), threads or (os.cpu_count() or 1), m_off, bins,
+                                          _ptr(counts), _ptr(exact)))
+        return counts, exact
 
     def norm(self):
         out, ex = C.c_double(), C.c_double()
@@ -259,6 +303,20 @@ class OracleState:
         sec, cs = C.c_double(), C.c_double()
         _check(lib().orc_time_pairs(self._h, C.byref(st), num_pairs, seed, threads, C.byref(sec), C.byref(cs)))
         return sec.value, cs.value
+
+
+def t_tensor_rank(t: int) -> int:
+    v = C.c_uint64()
+    _check(lib().orc_t_tensor_rank(t, C.byref(v)))
+    return v.value
+
+
+def counts_value(counts, m_off: int) -> float:
+    """Σ_m counts[m + m_off]·2^(-m/2), evaluated exactly by the oracle."""
+    c = np.ascontiguousarray(counts, dtype=np.int64)
+    v = C.c_double()
+    _check(lib().orc_counts_value(_ptr(c), m_off, len(c), C.byref(v)))
+    return v.value
 
 
 def random_clifford(n: int, seed: bytes | None) -> np.ndarray:

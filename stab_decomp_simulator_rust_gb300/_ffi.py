@@ -90,6 +90,12 @@ def load(path: str | None = None):
     L.nsg_profile_enable.argtypes = [i32]
     L.nsg_profile_read.argtypes = [P(dbl), P(u64), P(u64)]
     L.nsg_probe_int_ops.argtypes = [u64, P(dbl), P(u64)]
+    L.nsg_exp_value_counts.argtypes = [vp, P(PauliABI), sz, vp, P(dbl)]
+    L.nsg_set_pair_tiling.argtypes = [i32, i32]
+    L.nsg_debug_compile_keep.argtypes = [u32, vp, sz, vp, sz, P(u64)]
+    L.nsg_state_select.argtypes = [vp, vp, sz, P(vp)]
+    L.nsg_debug_set_wait.argtypes = [u32, u32]
+    L.nsg_states_from_circuits.argtypes = [sz, vp, vp, vp, vp]
     for name in header_symbols():
         fn = getattr(L, name)
         if name not in ("nsg_version", "nsg_last_error_message", "nsg_state_free", "nsg_plan_free"):

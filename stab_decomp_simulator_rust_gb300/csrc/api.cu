@@ -517,6 +517,9 @@ struct nsg_state {
                 raise(NSG_ERR_CANNOT_DISCARD_QUBIT, qubit, -1, "Cannot discard qubit %lld because it is not in a proper state",
                       (long long)qubit);
             if (h[0] & DS_TIMEOUT) raise(NSG_ERR_TIMEOUT, h[0], -1, "a bounded device wait ran out (status %d)", h[0]);
+            if (h[0] == DS_RANGE)
+                raise(NSG_ERR_INVALID_ARGUMENT, h[0], -1,
+                      "a pair term's exponent fell outside the exact count bins (status %d)", h[0]);
             raise(NSG_ERR_DEVICE_INVARIANT, h[0], -1, "device invariant violated (status %d; at %d %d %d)", h[0], h[2],
                   h[3], h[4]);
         }
@@ -599,6 +602,7 @@ struct PairUnit {
     bool triangular = true;
     bool complex_out = false;
     double* out = nullptr;  // host: nobs values, or nobs (re, im) pairs when complex_out
+    int64_t* counts = nullptr;  // exact mode (host): [nobs][2][kExactBins] signed counts (re, im)
 };
 
 constexpr int kMaxObsPerUnit = 256;  // 8 observable groups of 32 lanes
@@ -714,6 +718,17 @@ struct PairTiling {
     int minb[2] = {0, 0};
 };
 
+// The tiling of direct (uncaptured) pair sums: the defaults, or the values set
+// by nsg_set_pair_tiling (0 keeps a default).
+std::mutex g_tiling_mu;
+PairTiling g_tiling_override;
+PairTiling pair_tiling_override() {
+    std::lock_guard<std::mutex> lk(g_tiling_mu);
+    return g_tiling_override;
+}
+// Barrier-wait settings of the pair launches (nsg_debug_set_wait).
+uint32_t g_poll_limit = 0, g_extra_tx = 0;
+
 // Everything one batched evaluation needs on the device, built once
 // (descriptors uploaded) and enqueued any number of times.
 struct PairBatch {
@@ -739,14 +754,17 @@ struct PairBatch {
     DBuf<uint8_t> pk;
     std::vector<Launch> launches;
     DBuf<double> dout;  // (re, im) per observable, launches concatenated
+    DBuf<unsigned long long> dcounts;  // exact mode: [tot_obs][2][kExactBins]
+    bool exact = false;
     size_t tot_obs = 0;
     uint64_t pairs = 0;
 };
 
 // with_samples: also the pair counts of the first tasks (for timing samples).
 void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st, bool with_samples = false,
-                 uint8_t* dbg_k = nullptr, int32_t* dbg_r = nullptr) {
+                 uint8_t* dbg_k = nullptr, int32_t* dbg_r = nullptr, bool exact = false) {
     const size_t L = b.live.size();
+    b.exact = exact;
     b.tot_obs = 0;
     size_t tot_px = 0;
     b.unit_obs.assign(L, 0);
@@ -766,6 +784,7 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
     b.px.alloc(std::max<size_t>(tot_px, 1), st);
     b.pk.alloc(std::max<size_t>(tot_px, 1), st);
     b.dout.alloc(2 * std::max<size_t>(b.tot_obs, 1), st);
+    if (exact) b.dcounts.alloc(std::max<size_t>(b.tot_obs, 1) * 2 * kExactBins, st);
     b.launches.clear();
     b.pairs = 0;
     size_t out_base = 0;
@@ -805,6 +824,7 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
             d.triangular = u->triangular ? 1 : 0;
             d.complex_out = u->complex_out ? 1 : 0;
             d.status = u->a->status.p;
+            if (exact) d.counts = b.dcounts.p + b.unit_obs[sel[q]] * 2 * kExactBins;
             if (u->complex_out) {  // conj(g_a)·g_b (stabilizer_decomposed_state/inner_product.rs:18)
                 d.scale_re = u->a->gf_re * u->b->gf_re + u->a->gf_im * u->b->gf_im;
                 d.scale_im = u->a->gf_re * u->b->gf_im - u->a->gf_im * u->b->gf_re;
@@ -841,7 +861,7 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
                 raise(NSG_ERR_INVALID_ARGUMENT, nobs_max, 32, "complex pair sums take at most 32 observables per launch");
         // Tasks: about tasks_per_warp per resident warp, never spanning two units.
         const size_t warp_smem = pair_warp_smem_bytes(tab_max, bra_max, wb);
-        int minb = tl.minb[wb == 4 ? 0 : 1];
+        int minb = exact ? -1 : tl.minb[wb == 4 ? 0 : 1];
         if (minb == 0) {
             uint64_t pairs = 0, nsum = 0;
             for (size_t q = 0; q < sel.size(); q++) {
@@ -854,7 +874,7 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
             const int n_mean = pairs ? (int)(nsum / pairs) : 0;
             if (!tune_lookup(tune_key(dev, wb, nobs_max, n_mean, pairs), minb)) minb = default_minb(wb, nobs_max, n_mean);
         }
-        const int64_t resident = pair_resident_warps(wb, nobs_max, warp_smem, minb);
+        const int64_t resident = pair_resident_warps(wb, nobs_max, warp_smem, exact ? 0 : minb);
         int64_t total_chunks = 0;
         for (const PairDesc& d : descs) total_chunks += d.nchunks;
         const int64_t want = (int64_t)tl.tasks_per_warp * resident;
@@ -923,11 +943,17 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
         m.chunk = tl.chunk;
         m.nobs_max = nobs_max;
         m.mixed = mixed;
+        m.exact = exact;
+        {
+            std::lock_guard<std::mutex> lk(g_tiling_mu);
+            m.poll_limit = g_poll_limit;
+            m.dbg_extra_tx = g_extra_tx;
+        }
         const int wpb = 4;  // warps per block of the pair kernel
         const int64_t warps = std::min<int64_t>(total_tasks, resident);
         m.blocks = (int)std::max<int64_t>(1, (warps + wpb - 1) / wpb);
         m.nwarps = m.blocks * wpb;
-        m.minb = minb;
+        m.minb = exact ? 2 : minb;
         m.tab_bytes_max = tab_max;
         m.bra_bytes_max = bra_max;
         m.warp_smem = warp_smem;
@@ -952,6 +978,7 @@ void enqueue_batch(PairBatch& b, cudaStream_t st, float* pair_ms = nullptr, int6
     for (size_t k = 0; k < b.live.size(); k++)
         CK(launch_pauli_frames(b.live[k]->a->t.view(), b.dp.p + b.unit_obs[k], b.live[k]->nobs,
                                b.px.p + b.unit_px[k], b.pk.p + b.unit_px[k], st));
+    if (b.exact) CK(cudaMemsetAsync(b.dcounts.p, 0, b.dcounts.n * sizeof(unsigned long long), st));
     for (PairBatch::Launch& ln : b.launches) {
         CK(cudaMemsetAsync(ln.rec.p, 0, ln.rec_used * sizeof(double), st));
         MultiLaunch m = ln.m;
@@ -977,7 +1004,8 @@ void enqueue_batch(PairBatch& b, cudaStream_t st, float* pair_ms = nullptr, int6
             cudaEventDestroy(ev1);
             *pair_ms += ms;
         }
-        CK(launch_reduce_multi(m, ln.d_obegin, ln.obegin.back(), b.dout.p + 2 * ln.out_off, ln.red_scratch, st));
+        if (!b.exact)
+            CK(launch_reduce_multi(m, ln.d_obegin, ln.obegin.back(), b.dout.p + 2 * ln.out_off, ln.red_scratch, st));
     }
 }
 
@@ -1021,7 +1049,7 @@ std::vector<nsg_state*> distinct_states(const std::vector<PairUnit*>& live) {
 // launch; all of it on `st`.  Bra frames and term tables are built (once per
 // state, cached) on each state's own stream and joined into `st`.
 void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, uint8_t* dbg_k = nullptr,
-                    int32_t* dbg_r = nullptr) {
+                    int32_t* dbg_r = nullptr, bool exact = false) {
     PairBatch b;
     b.live = live_units(units);
     if (b.live.empty()) return;
@@ -1034,7 +1062,7 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
     }
     const std::vector<nsg_state*> touched = distinct_states(b.live);
     for (nsg_state* s : touched) join_stream(st, s->st);
-    build_batch(b, PairTiling(), mixed, st, false, dbg_k, dbg_r);
+    build_batch(b, pair_tiling_override(), mixed, st, false, dbg_k, dbg_r, exact);
     bool prof;
     {
         std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -1043,7 +1071,11 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
     float prof_ms = 0.f;
     enqueue_batch(b, st, prof ? &prof_ms : nullptr);
     std::vector<double> hout(2 * b.tot_obs);
-    CK(cudaMemcpyAsync(hout.data(), b.dout.p, hout.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+    std::vector<int64_t> hcounts(exact ? b.tot_obs * 2 * kExactBins : 0);
+    if (exact)
+        CK(cudaMemcpyAsync(hcounts.data(), b.dcounts.p, hcounts.size() * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    else
+        CK(cudaMemcpyAsync(hout.data(), b.dout.p, hout.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
     if (prof) {
         std::lock_guard<std::mutex> lk(g_prof_mu);
@@ -1051,7 +1083,14 @@ void run_pair_units(std::vector<PairUnit>& units, bool mixed, cudaStream_t st, u
         g_prof_launches += b.launches.size();
         g_prof_pairs += b.pairs;
     }
-    scatter_batch(b, hout.data());
+    if (exact) {
+        for (size_t k = 0; k < b.live.size(); k++)
+            if (b.live[k]->counts)
+                std::memcpy(b.live[k]->counts, hcounts.data() + b.unit_obs[k] * 2 * kExactBins,
+                            (size_t)b.live[k]->nobs * 2 * kExactBins * sizeof(int64_t));
+    } else {
+        scatter_batch(b, hout.data());
+    }
     // The launches ran on `st`; each bra state's status words report its units.
     for (nsg_state* s : touched) s->check_status();
 }
@@ -1349,10 +1388,24 @@ nsg_status nsg_last_error_args(int64_t out[3]) {
     return NSG_OK;
 }
 
-nsg_status nsg_state_from_circuit(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates, nsg_state** out) {
-    API_BEGIN
-    need(out, "out");
-    *out = nullptr;
+namespace {
+// StabDecompCompiler::compile (compiler/mod.rs:44-140) on the device, in two
+// phases so that many circuits can be enqueued before any host wait:
+// compile_enqueue lowers the circuit (with the reference's checks, in its
+// order), creates the state and queues the compile kernel and the stable
+// compaction of the kept terms on the state's stream; compile_finish waits for
+// that stream and installs the compacted terms.
+struct PendingCompile {
+    std::unique_ptr<nsg_state> s;
+    TermStore out;               // the compaction's target
+    DBuf<int32_t> keep, pos;
+    DBuf<int64_t> cnt;
+    DBuf<uint32_t> dops;
+    int64_t chi_t = 0;
+    int64_t* h_count = nullptr;  // pinned slot the kept count is copied to
+};
+
+void compile_enqueue(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates, PendingCompile& pc) {
     if (num_gates) need(gates, "gates");
     const int n = (int)num_qubits;
     // Lowering (compiler/mod.rs:49-63): T/Tdg -> CX(target, n+k) [+ Sdg(target)].
@@ -1385,23 +1438,151 @@ nsg_status nsg_state_from_circuit(uint32_t num_qubits, const nsg_gate* gates, si
             lower_clifford(g, width, ops);
         }
     }
-    auto s = std::make_unique<nsg_state>();
+    pc.s = std::make_unique<nsg_state>();
+    nsg_state* s = pc.s.get();
     s->init_stream();
     cudaStream_t st = s->st;
     auto tt = t_tensor_dev(t, st, s->status.p);
-    DBuf<uint32_t> dops;
-    dops.alloc(std::max<size_t>(ops.size(), 1), st);
-    if (!ops.empty()) CK(cudaMemcpyAsync(dops.p, ops.data(), ops.size() * 4, cudaMemcpyHostToDevice, st));
+    pc.chi_t = tt->chi;
+    pc.dops.alloc(std::max<size_t>(ops.size(), 1), st);
+    if (!ops.empty()) CK(cudaMemcpyAsync(pc.dops.p, ops.data(), ops.size() * 4, cudaMemcpyHostToDevice, st));
     TermStore raw;
     raw.alloc(n, tt->chi, st);
     raw.chi = tt->chi;
-    DBuf<int32_t> keep;
-    keep.alloc(tt->chi, st);
+    pc.keep.alloc(tt->chi, st);
     TermsView rv = raw.view();
-    CK(launch_compile(dops.p, (int)ops.size(), n, t, tt->chi, tt->G, tt->F, tt->M, tt->gam, tt->V, tt->S, tt->phase,
-                      tt->ck, tt->cr, rv, keep.p, s->status.p, st));
+    CK(launch_compile(pc.dops.p, (int)ops.size(), n, t, tt->chi, tt->G, tt->F, tt->M, tt->gam, tt->V, tt->S,
+                      tt->phase, tt->ck, tt->cr, rv, pc.keep.p, s->status.p, st));
     s->t = std::move(raw);
+    pc.out.alloc(s->t.n, std::max<int64_t>(s->t.chi, 1), st);
+    pc.out.W = s->t.W;
+    pc.out.R = s->t.R;
+    pc.pos.alloc(std::max<int64_t>(s->t.chi, 1), st);
+    pc.cnt.alloc(1, st);
+    CK(launch_compact(s->t.view(), pc.keep.p, pc.pos.p, pc.out.view(), pc.cnt.p, st));
+    CK(cudaMemcpyAsync(pc.h_count, pc.cnt.p, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+}
+
+void compile_finish(PendingCompile& pc, std::vector<uint8_t>* keep_out) {
+    nsg_state* s = pc.s.get();
+    CK(cudaStreamSynchronize(s->st));
     s->check_status();
+    if (keep_out) {
+        std::vector<int32_t> hk((size_t)pc.chi_t);
+        CK(cudaMemcpyAsync(hk.data(), pc.keep.p, hk.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+        CK(cudaStreamSynchronize(s->st));
+        keep_out->assign(hk.size(), 0);
+        for (size_t i = 0; i < hk.size(); i++) (*keep_out)[i] = hk[i] ? 1 : 0;
+    }
+    pc.out.chi = *pc.h_count;
+    s->t = std::move(pc.out);
+    s->layout_gen++;
+    s->invalidate();
+    pc.keep.release();
+    pc.pos.release();
+    pc.cnt.release();
+    pc.dops.release();
+}
+
+// Pinned host slots for the kept counts of a compile batch.
+struct PinnedCounts {
+    int64_t* p = nullptr;
+    explicit PinnedCounts(size_t n) { CK(cudaMallocHost((void**)&p, std::max<size_t>(n, 1) * sizeof(int64_t))); }
+    ~PinnedCounts() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+std::unique_ptr<nsg_state> compile_state(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates,
+                                         std::vector<uint8_t>* keep_out) {
+    int64_t count = 0;
+    PendingCompile pc;
+    pc.h_count = &count;  // pageable: the copy completes before the stream wait returns
+    compile_enqueue(num_qubits, gates, num_gates, pc);
+    compile_finish(pc, keep_out);
+    return std::move(pc.s);
+}
+}  // namespace
+
+nsg_status nsg_state_from_circuit(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates, nsg_state** out) {
+    API_BEGIN
+    need(out, "out");
+    *out = nullptr;
+    *out = compile_state(num_qubits, gates, num_gates, nullptr).release();
+    API_END
+}
+
+nsg_status nsg_states_from_circuits(size_t num_circuits, const uint32_t* num_qubits, const nsg_gate* const* gates,
+                                    const size_t* num_gates, nsg_state** out) {
+    API_BEGIN
+    if (num_circuits) {
+        need(num_qubits, "num_qubits");
+        need(gates, "gates");
+        need(num_gates, "num_gates");
+        need(out, "out");
+    }
+    for (size_t c = 0; c < num_circuits; c++) out[c] = nullptr;
+    PinnedCounts counts(num_circuits);
+    std::vector<PendingCompile> pend(num_circuits);
+    for (size_t c = 0; c < num_circuits; c++) {
+        pend[c].h_count = counts.p + c;
+        try {
+            compile_enqueue(num_qubits[c], gates[c], num_gates[c], pend[c]);
+        } catch (const ApiError& e) {
+            g_args[2] = (int64_t)c;  // the failing circuit
+            for (size_t j = 0; j < c; j++) CK(cudaStreamSynchronize(pend[j].s->st));
+            throw;
+        }
+    }
+    for (size_t c = 0; c < num_circuits; c++) {
+        try {
+            compile_finish(pend[c], nullptr);
+        } catch (const ApiError& e) {
+            g_args[2] = (int64_t)c;
+            for (size_t j = c + 1; j < num_circuits; j++) CK(cudaStreamSynchronize(pend[j].s->st));
+            throw;
+        }
+    }
+    for (size_t c = 0; c < num_circuits; c++) out[c] = pend[c].s.release();
+    API_END
+}
+
+nsg_status nsg_debug_compile_keep(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates, uint8_t* keep,
+                                  size_t capacity, uint64_t* num_t_terms) {
+    API_BEGIN
+    need(num_t_terms, "num_t_terms");
+    std::vector<uint8_t> k;
+    std::unique_ptr<nsg_state> s = compile_state(num_qubits, gates, num_gates, &k);
+    *num_t_terms = k.size();
+    if (k.size() > capacity) raise(NSG_ERR_BUFFER_TOO_SMALL, (int64_t)k.size(), (int64_t)capacity, "keep buffer too small");
+    if (!k.empty()) {
+        need(keep, "keep");
+        std::memcpy(keep, k.data(), k.size());
+    }
+    API_END
+}
+
+nsg_status nsg_state_select(const nsg_state* cstate, const uint64_t* indices, size_t count, nsg_state** out) {
+    API_BEGIN
+    need(cstate, "state");
+    need(out, "out");
+    *out = nullptr;
+    if (count) need(indices, "indices");
+    DeviceScope ds_(cstate->device);
+    for (size_t i = 0; i < count; i++) {
+        if ((int64_t)indices[i] >= cstate->t.chi)
+            raise(NSG_ERR_QUBIT_INDEX_OUT_OF_BOUNDS, (int64_t)indices[i], cstate->t.chi, "term index %llu out of range",
+                  (unsigned long long)indices[i]);
+        if (i && indices[i] <= indices[i - 1])
+            raise(NSG_ERR_INVALID_ARGUMENT, (int64_t)i, -1, "term indices must be strictly ascending");
+    }
+    nsg_state* src = const_cast<nsg_state*>(cstate);
+    auto s = std::unique_ptr<nsg_state>(clone_state(src));
+    std::vector<int32_t> hk((size_t)std::max<int64_t>(s->t.chi, 1), 0);
+    for (size_t i = 0; i < count; i++) hk[indices[i]] = 1;
+    DBuf<int32_t> keep;
+    keep.alloc(hk.size(), s->st);
+    CK(cudaMemcpyAsync(keep.p, hk.data(), hk.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
     compact_into(s.get(), keep);
     *out = s.release();
     API_END
@@ -1616,6 +1797,62 @@ nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states
         DeviceScope ds_(states[0]->device);
         run_pair_units(units, precision == NSG_PRECISION_MIXED, const_cast<nsg_state*>(states[0])->st);
     }
+    API_END
+}
+
+nsg_status nsg_exp_value_counts(const nsg_state* cstate, const nsg_pauli* paulis, size_t num_paulis, int64_t* counts,
+                                double* scale) {
+    API_BEGIN
+    need(cstate, "state");
+    DeviceScope ds_(cstate->device);
+    if (num_paulis) {
+        need(paulis, "paulis");
+        need(counts, "counts");
+    }
+    nsg_state* state = const_cast<nsg_state*>(cstate);
+    require_pairs_width(state);
+    std::vector<DevPauli> dp(num_paulis);
+    for (size_t i = 0; i < num_paulis; i++) dp[i] = to_dev_pauli(paulis[i], state->t.n);
+    if (num_paulis) std::memset(counts, 0, num_paulis * kExactBins * sizeof(int64_t));
+    std::vector<int64_t> both(2 * kExactBins * std::min<size_t>(num_paulis, kMaxObsPerUnit));
+    std::vector<double> unused(std::max<size_t>(num_paulis, 1));
+    for (size_t base = 0; base < num_paulis; base += kMaxObsPerUnit) {
+        std::vector<PairUnit> units(1);
+        PairUnit& u = units[0];
+        u.a = state;
+        u.b = state;
+        u.paulis = dp.data() + base;
+        u.nobs = (int)std::min<size_t>(kMaxObsPerUnit, num_paulis - base);
+        u.triangular = true;
+        u.out = unused.data() + base;
+        std::fill(both.begin(), both.end(), 0);
+        u.counts = both.data();
+        run_pair_units(units, false, state->st, nullptr, nullptr, true);
+        for (int o = 0; o < u.nobs; o++)  // the real-part bins of each observable
+            std::memcpy(counts + (base + o) * kExactBins, both.data() + (size_t)o * 2 * kExactBins,
+                        kExactBins * sizeof(int64_t));
+    }
+    if (scale) *scale = state->gf_re * state->gf_re + state->gf_im * state->gf_im;
+    API_END
+}
+
+nsg_status nsg_set_pair_tiling(int32_t chunk, int32_t tasks_per_warp) {
+    API_BEGIN
+    if (chunk < 0 || chunk > 1024 || tasks_per_warp < 0 || tasks_per_warp > 1024)
+        raise(NSG_ERR_INVALID_ARGUMENT, chunk, tasks_per_warp, "tiling out of range");
+    std::lock_guard<std::mutex> lk(g_tiling_mu);
+    const PairTiling def;
+    g_tiling_override.chunk = chunk ? chunk : def.chunk;
+    g_tiling_override.tasks_per_warp = tasks_per_warp ? tasks_per_warp : def.tasks_per_warp;
+    API_END
+}
+
+nsg_status nsg_debug_set_wait(uint32_t poll_limit, uint32_t extra_tx_bytes) {
+    API_BEGIN
+    if (extra_tx_bytes > 1024) raise(NSG_ERR_INVALID_ARGUMENT, extra_tx_bytes, 1024, "extra bytes out of range");
+    std::lock_guard<std::mutex> lk(g_tiling_mu);
+    g_poll_limit = poll_limit;
+    g_extra_tx = extra_tx_bytes;
     API_END
 }
 

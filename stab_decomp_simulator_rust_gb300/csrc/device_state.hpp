@@ -67,7 +67,13 @@ enum DevStatus : int {
     DS_INVARIANT = 1,  // reference panic paths
     DS_CANNOT_DISCARD = 2,
     DS_TIMEOUT = 4,  // a bounded wait on a shared-memory barrier ran out
+    DS_RANGE = 8,    // an exact count fell outside the count bins
 };
+
+// Exact accumulation: signed counts of pair-term real (and imaginary) parts
+// sign·2^{-m/2} per m, at index m + kExactMOffset of kExactBins bins.
+constexpr int kExactBins = 512;
+constexpr int kExactMOffset = 192;
 
 // ---- launchers (kernels_*.cu) ------------------------------------------------
 
@@ -188,6 +194,7 @@ struct PairDesc {
     int64_t rec0 = 0;                        // first double of the unit's task records
     double scale_re = 1.0, scale_im = 0.0;   // |g|² or conj(g_a)·g_b
     int* status = nullptr;                   // the owning state's status words
+    unsigned long long* counts = nullptr;    // exact mode: [nobs][2][kExactBins] signed counts (re, im)
 };
 
 // A persistent launch over the task lists of many units.  Each unit's chunks
@@ -204,6 +211,7 @@ struct MultiLaunch {
     int chunk = 32;
     int nobs_max = 1;
     bool mixed = false;
+    bool exact = false;                   // integer counts per power of √2 instead of FP sums (descs[].counts)
     double* records = nullptr;
     unsigned long long* counter = nullptr;  // zero before the launch
     int nwarps = 0;
@@ -214,6 +222,8 @@ struct MultiLaunch {
     size_t warp_smem = 0;
     uint8_t* dbg_k = nullptr;             // single-unit per-pair dump [chiA][chiB]
     int32_t* dbg_r = nullptr;
+    uint32_t poll_limit = 0;              // polls of a bounded barrier wait (0: 2^22)
+    uint32_t dbg_extra_tx = 0;            // test hook: bytes a chunk's first ket barrier expects beyond its copy
 };
 
 // word_bytes: 4 when every unit of the launch has n ≤ 32, 8 when every unit

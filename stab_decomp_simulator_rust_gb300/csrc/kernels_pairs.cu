@@ -361,9 +361,12 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar) {
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 
-// One elected lane: arm the barrier for `bytes` and start the bulk copy.
-__device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+// One elected lane: arm the barrier for `bytes` (+ `extra`, a test hook that
+// leaves the phase incomplete after the copy has landed) and start the bulk
+// copy of `bytes`.
+__device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar,
+                                         uint32_t extra = 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes + extra)
                  : "memory");
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_u32(dst)),
@@ -372,8 +375,8 @@ __device__ __forceinline__ void tma_load(void* dst, const void* src, uint32_t by
 }
 
 // Bounded wait on a barrier phase; false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-    for (int it = 0; it < (1 << 22); it++) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+    for (uint32_t it = 0; it < limit; it++) {
         uint32_t done;
         asm volatile(
             "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
@@ -478,7 +481,27 @@ __device__ __forceinline__ void g_subst(int kq, Word lp, const bool (&c)[NG], Wo
 // MINB: blocks per SM the register allocation must allow (the register cap is
 // 65536 / (128·MINB)); the launch picks it per workload (fewer blocks leave
 // more registers for many observables per lane).
-template <typename Word, int RPL, int NG, int MINB>
+// Exact mode: one signed count per (observable, power of √2) in global
+// memory (integer atomics, so the result does not depend on the schedule);
+// a lane merges consecutive terms of one observable that fall in the same bin.
+__device__ __forceinline__ void exact_flush(unsigned long long* bins, int& bin, int& cnt) {
+    if (cnt) atomicAdd(bins + bin, (unsigned long long)(long long)cnt);
+    cnt = 0;
+}
+__device__ __forceinline__ void exact_add(unsigned long long* bins, int& bin, int& cnt, int m, int v, int* status) {
+    const int b = m + kExactMOffset;
+    if (b < 0 || b >= kExactBins) {
+        atomicOr(status, DS_RANGE);
+        return;
+    }
+    if (b != bin) {
+        exact_flush(bins, bin, cnt);
+        bin = b;
+    }
+    cnt += v;
+}
+
+template <typename Word, int RPL, int NG, int MINB, bool EXACT>
 __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) {
     constexpr int GMAX = (8 * sizeof(Word)) / 4;  // groups of four rows (8 or 16)
     // Unrolling of the table-lookup loops: full for 32-bit rows; for 64-bit
@@ -526,6 +549,7 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
     int ks[NG];
     int buf = 0;
     bool timed_out = false;
+    const uint32_t polls = p.poll_limit ? p.poll_limit : (1u << 22);
 
     // Work queue: the first task of every warp is its own index, the next
     // ones come from a global counter.  A task is a run of at most
@@ -604,11 +628,17 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
             constexpr int NA = (NG == 1) ? 4 : 2;
             ChunkAcc<NG, NA> acc;
             acc.reset();
+            int ex_bin[EXACT ? NG : 1], ex_cnt[EXACT ? NG : 1];
+            if constexpr (EXACT) {
+#pragma unroll
+                for (int g = 0; g < NG; g++) ex_bin[g] = ex_cnt[g] = 0;
+            }
 
             // first ket of the chunk
             if (lane == 0) {
                 fence_proxy_async();
-                tma_load(buf ? tb1 : tb0, ktab + (size_t)j0 * d->ktab_stride, tab_bytes, buf ? &bars[1] : &bars[0]);
+                tma_load(buf ? tb1 : tb0, ktab + (size_t)j0 * d->ktab_stride, tab_bytes, buf ? &bars[1] : &bars[0],
+                         p.dbg_extra_tx);
             }
             for (int64_t j = j0; j < j1; j++) {
                 // prefetch the next ket's tables into the other buffer
@@ -619,10 +649,10 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                 }
                 bool ok_wait;
                 if (buf) {
-                    ok_wait = mbar_wait(&bars[1], par1);
+                    ok_wait = mbar_wait(&bars[1], par1, polls);
                     par1 ^= 1;
                 } else {
-                    ok_wait = mbar_wait(&bars[0], par0);
+                    ok_wait = mbar_wait(&bars[0], par0, polls);
                     par0 ^= 1;
                 }
                 if (!ok_wait) {
@@ -630,8 +660,8 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                     // buffer (if one was issued) a bounded wait before leaving.
                     if (lane == 0) atomicOr(d->status, DS_TIMEOUT);
                     if (j + 1 < j1) {
-                        if (buf) mbar_wait(&bars[0], par0);
-                        else mbar_wait(&bars[1], par1);
+                        if (buf) mbar_wait(&bars[0], par0, 1u << 22);
+                        else mbar_wait(&bars[1], par1, 1u << 22);
                     }
                     timed_out = true;
                     break;
@@ -820,16 +850,29 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         p.dbg_r[di] = r;
                     }
                     if (!zero[g] && o < nobs) {
-                        double* pp = rec + (size_t)o * 8;
                         const int k = (kpair + ks[g] + ph[g]) & 7;
                         int sgn, m;
                         re_part(k, rpair, sgn, m);
-                        if (sgn) acc.add(g, m & 1, sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1), p.mixed, pp);
-                        if (NA == 4 && cplx) {
-                            im_part(k, rpair, sgn, m);
-                            if (sgn)
-                                acc.add(g, (NA == 4 ? 2 : 0) + (m & 1), sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1),
-                                        p.mixed, pp);
+                        if constexpr (EXACT) {
+                            unsigned long long* bins = d->counts + (size_t)o * 2 * kExactBins;
+                            if (sgn) exact_add(bins, ex_bin[g], ex_cnt[g], m, sgn * wgt, d->status);
+                            if (cplx) {
+                                im_part(k, rpair, sgn, m);
+                                const int b = m + kExactMOffset;
+                                if (sgn && b >= 0 && b < kExactBins)
+                                    atomicAdd(bins + kExactBins + b, (unsigned long long)(long long)(sgn * wgt));
+                                else if (sgn)
+                                    atomicOr(d->status, DS_RANGE);
+                            }
+                        } else {
+                            double* pp = rec + (size_t)o * 8;
+                            if (sgn) acc.add(g, m & 1, sgn * wgt, (m & 1) ? ((m - 1) >> 1) : (m >> 1), p.mixed, pp);
+                            if (NA == 4 && cplx) {
+                                im_part(k, rpair, sgn, m);
+                                if (sgn)
+                                    acc.add(g, (NA == 4 ? 2 : 0) + (m & 1), sgn * wgt,
+                                            (m & 1) ? ((m - 1) >> 1) : (m >> 1), p.mixed, pp);
+                            }
                         }
                     }
                 }
@@ -840,7 +883,11 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
 #pragma unroll
             for (int g = 0; g < NG; g++) {
                 const int o = 32 * g + lane;
-                if (o < nobs) acc.flush_group(g, rec + (size_t)o * 8, p.mixed);
+                if constexpr (EXACT) {
+                    if (o < nobs) exact_flush(d->counts + (size_t)o * 2 * kExactBins, ex_bin[g], ex_cnt[g]);
+                } else {
+                    if (o < nobs) acc.flush_group(g, rec + (size_t)o * 8, p.mixed);
+                }
             }
         }
         unsigned long long next = 0;
@@ -1193,28 +1240,31 @@ __global__ void reduce_kernel(const double* __restrict__ partials, int nwarps, i
 // Dynamic shared memory above 48 KB needs an opt-in per kernel (and device);
 // it is set outside stream capture (the first launch of a shape is never a
 // captured one: plans run once before they capture).
-template <typename Word, int RPL, int NG, int MINB>
+template <typename Word, int RPL, int NG, int MINB, bool EXACT = false>
 cudaError_t allow_smem(size_t smem, cudaStream_t st) {
     if (smem <= 48 * 1024) return cudaSuccess;
     if (st) {
         cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
         if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) return cudaSuccess;
     }
-    return cudaFuncSetAttribute(pair_kernel<Word, RPL, NG, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    return cudaFuncSetAttribute(pair_kernel<Word, RPL, NG, MINB, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)smem);
 }
 
-template <typename Word, int RPL, int NG, int MINB>
+template <typename Word, int RPL, int NG, int MINB, bool EXACT = false>
 cudaError_t launch_pairs_ng(const MultiLaunch& p, cudaStream_t st) {
     const size_t smem = (size_t)p.warp_smem * PWARPS;
-    cudaError_t e = allow_smem<Word, RPL, NG, MINB>(smem, st);
+    cudaError_t e = allow_smem<Word, RPL, NG, MINB, EXACT>(smem, st);
     if (e != cudaSuccess) return e;
-    pair_kernel<Word, RPL, NG, MINB><<<p.blocks, PWARPS * 32, smem, st>>>(p);
+    pair_kernel<Word, RPL, NG, MINB, EXACT><<<p.blocks, PWARPS * 32, smem, st>>>(p);
     return cudaGetLastError();
 }
 
+// The exact-count mode has one variant per row width and observable groups
+// (the largest register budget, two blocks per SM).
 template <typename Word, int RPL, int NG>
 cudaError_t launch_pairs_minb(const MultiLaunch& p, cudaStream_t st) {
+    if (p.exact) return launch_pairs_ng<Word, RPL, NG, 2, true>(p, st);
     switch (p.minb) {
         case 2: return launch_pairs_ng<Word, RPL, NG, 2>(p, st);
         case 3: return launch_pairs_ng<Word, RPL, NG, 3>(p, st);
@@ -1223,11 +1273,11 @@ cudaError_t launch_pairs_minb(const MultiLaunch& p, cudaStream_t st) {
     }
 }
 
-template <typename Word, int RPL, int NG, int MINB>
+template <typename Word, int RPL, int NG, int MINB, bool EXACT = false>
 int resident_blocks_ng(size_t warp_smem) {
     int nb = 0;
-    if (allow_smem<Word, RPL, NG, MINB>(warp_smem * PWARPS, nullptr) != cudaSuccess) return 1;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pair_kernel<Word, RPL, NG, MINB>, PWARPS * 32,
+    if (allow_smem<Word, RPL, NG, MINB, EXACT>(warp_smem * PWARPS, nullptr) != cudaSuccess) return 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, pair_kernel<Word, RPL, NG, MINB, EXACT>, PWARPS * 32,
                                                       warp_smem * PWARPS) != cudaSuccess)
         return 1;
     return nb > 0 ? nb : 1;
@@ -1235,6 +1285,7 @@ int resident_blocks_ng(size_t warp_smem) {
 
 template <typename Word, int RPL, int NG>
 int resident_blocks_minb(size_t warp_smem, int minb) {
+    if (minb == 0) return resident_blocks_ng<Word, RPL, NG, 2, true>(warp_smem);  // exact mode
     switch (minb) {
         case 2: return resident_blocks_ng<Word, RPL, NG, 2>(warp_smem);
         case 3: return resident_blocks_ng<Word, RPL, NG, 3>(warp_smem);

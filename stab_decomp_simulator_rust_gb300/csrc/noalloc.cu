@@ -11,16 +11,22 @@
 // device array, g_noalloc_scratch, of 16 MiB.  Every GPU that loads the
 // library holds that array until the process exits.
 //
-// Limits: n ≤ 64 qubits and χ ≤ 8192 terms (the frames of 8192 terms plus
-// the pair-kernel partials fit the 16 MiB); larger states are rejected with
-// NSG_ERR_BUFFER_TOO_SMALL before anything runs.
+// Limits: n ≤ 64 qubits (NSG_ERR_TOO_WIDE above) and χ ≤ 8192 terms (the
+// frames of 8192 terms plus the pair-kernel partials fit the 16 MiB;
+// NSG_ERR_BUFFER_TOO_SMALL above), checked before anything runs.
 //
 // Set-up: the first call on a device looks up the array's device address
 // with cudaGetSymbolAddress (host code cannot use the symbol itself) and
 // caches it per device; make that first call before any stream capture.
-// All calls share the array and it keeps the previous call's contents: the
-// call clears the partial sums it accumulates into, and calls that overlap on
-// the GPU (two streams, two threads) race on the array.
+// CUDA loads a library's device code lazily by default, so the 16 MiB are
+// taken from the device when that first call runs (or when the module is
+// loaded for another reason): a caller whose memory another allocator will
+// reserve makes one call on each device before that allocator takes the
+// memory (or sets CUDA_MODULE_LOADING=EAGER).  The call runs on the state's
+// device and restores the caller's current device, like every other entry
+// point.  All calls share the array and it keeps the previous call's
+// contents: the call clears the partial sums it accumulates into, and calls
+// that overlap on the GPU (two streams, two threads) race on the array.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -74,6 +80,23 @@ nsg_status cuda_fail(cudaError_t e) {
     return NSG_ERR_CUDA;
 }
 
+// The state's device is current for the length of the call; the caller's is restored.
+struct DeviceSwitch {
+    int prev = -1;
+    cudaError_t err = cudaSuccess;
+    explicit DeviceSwitch(int dev) {
+        int cur = 0;
+        err = cudaGetDevice(&cur);
+        if (err == cudaSuccess && cur != dev) {
+            err = cudaSetDevice(dev);
+            if (err == cudaSuccess) prev = cur;
+        }
+    }
+    ~DeviceSwitch() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
 }  // namespace
 
 extern "C" nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pauli* pauli, double* out) {
@@ -83,14 +106,18 @@ extern "C" nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pa
     int* status = nullptr;
     int sdev = 0;
     double gf2 = 1.0;
-    state_internals(state, &tv, &st, &status, &sdev, &gf2);
+    if (!state_internals(state, &tv, &st, &status, &sdev, &gf2)) return fail(NSG_ERR_INVALID_ARGUMENT, "null state");
     const int n = tv.n;
     if (n > 64) return fail(NSG_ERR_TOO_WIDE, "nsg_exp_value_noalloc supports at most 64 qubits", n, 64);
     if (tv.chi > kMaxTerms)
         return fail(NSG_ERR_BUFFER_TOO_SMALL, "nsg_exp_value_noalloc supports at most 8192 terms", tv.chi, kMaxTerms);
 
-    // Pauli string -> bit form, with the length checks of exp_value.rs:9-27.
+    // Pauli string -> bit form, with the length checks of exp_value.rs:9-27
+    // and the argument checks of nsg_exp_value.
     DevPauli dp{0, 0, 0, 0};
+    if (pauli->len && !pauli->ops) return fail(NSG_ERR_INVALID_ARGUMENT, "null Pauli ops");
+    if (pauli->kind == NSG_PAULI_SPARSE && pauli->len && !pauli->qubits)
+        return fail(NSG_ERR_INVALID_ARGUMENT, "null Pauli qubits");
     if (pauli->kind == NSG_PAULI_DENSE) {
         if ((int)pauli->len != n) return fail(NSG_ERR_INVALID_PAULI_STRING_LENGTH, "Invalid Pauli string length.", n, pauli->len);
     } else if (pauli->kind == NSG_PAULI_SPARSE) {
@@ -115,11 +142,11 @@ extern "C" nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pa
     }
     dp.ny = e & 3;
 
-    int dev = 0;
-    cudaError_t ce = cudaGetDevice(&dev);
+    const int dev = sdev;
+    if (dev < 0 || dev >= kMaxDevices) return fail(NSG_ERR_INVALID_ARGUMENT, "device index too large", dev);
+    DeviceSwitch on_dev(dev);
+    cudaError_t ce = on_dev.err;
     if (ce != cudaSuccess) return cuda_fail(ce);
-    if (dev != sdev) return fail(NSG_ERR_INVALID_ARGUMENT, "the state lives on another device than the current one", sdev, dev);
-    if (dev >= kMaxDevices) return fail(NSG_ERR_INVALID_ARGUMENT, "device index too large", dev);
     unsigned char* base;
     {
         std::lock_guard<std::mutex> lk(g_setup_mu);
@@ -194,14 +221,16 @@ extern "C" nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pa
     if ((ce = launch_pairs_rows(pl, st)) != cudaSuccess) return cuda_fail(ce);
     if ((ce = launch_reduce(partials, pl.nwarps, 1, false, gf2, 0.0, dout, st)) != cudaSuccess) return cuda_fail(ce);
     double h = 0.0;
-    int hs = 0;
+    int hs[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // the state's status words (bits, detail claimed, detail)
     if ((ce = cudaMemcpyAsync(&h, dout, sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return cuda_fail(ce);
-    if ((ce = cudaMemcpyAsync(&hs, status, sizeof(int), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return cuda_fail(ce);
+    if ((ce = cudaMemcpyAsync(hs, status, sizeof(hs), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return cuda_fail(ce);
     if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(ce);
-    if (hs) {
-        cudaMemsetAsync(status, 0, sizeof(int), st);
-        cudaStreamSynchronize(st);
-        return fail(NSG_ERR_DEVICE_INVARIANT, "device invariant violated", hs);
+    if (hs[0]) {
+        if ((ce = cudaMemsetAsync(status, 0, sizeof(hs), st)) != cudaSuccess) return cuda_fail(ce);
+        if ((ce = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(ce);
+        if (hs[0] & DS_TIMEOUT) return fail(NSG_ERR_TIMEOUT, "a bounded device wait ran out", hs[0]);
+        if (hs[0] & DS_CANNOT_DISCARD) return fail(NSG_ERR_CANNOT_DISCARD_QUBIT, "cannot discard qubit", hs[0]);
+        return fail(NSG_ERR_DEVICE_INVARIANT, "device invariant violated", hs[0], hs[2]);
     }
     *out = h;
     return NSG_OK;

@@ -19,6 +19,44 @@ from .pauli import PauliString
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+EXACT_BINS = 512
+EXACT_M_OFFSET = 192
+
+
+def counts_to_xy(counts, m_offset: int = EXACT_M_OFFSET):
+    """The exact sum Σ_m counts[m + m_offset]·2^(-m/2) as X + Y/√2 with X, Y
+    dyadic rationals (even and odd m), returned as (X, Y) Fractions."""
+    from fractions import Fraction
+    X = Fraction(0)
+    Y = Fraction(0)
+    c = np.asarray(counts, dtype=np.int64)
+    for b in np.flatnonzero(c).tolist():
+        m = b - m_offset
+        e = m // 2 if m % 2 == 0 else (m - 1) // 2
+        v = Fraction(int(c[b])) / Fraction(2) ** e if e >= 0 else Fraction(int(c[b]) * 2 ** (-e))
+        if m % 2 == 0:
+            X += v
+        else:
+            Y += v
+    return X, Y
+
+
+def xy_to_float(X, Y, scale=1.0) -> float:
+    """scale·(X + Y/√2) rounded once: √2 is taken to 400 bits, far below the
+    last bit of a double."""
+    import math
+    from fractions import Fraction
+    if X == 0 and Y == 0:
+        return 0.0
+    P = 400
+    s2 = math.isqrt(2 << (2 * P))  # floor(√2·2^P)
+    return float((X * s2 + Y * (1 << P)) / s2 * Fraction(scale))
+
+
+def counts_to_value(counts, m_offset: int = EXACT_M_OFFSET, scale: float = 1.0) -> float:
+    """scale·Σ_m counts[m + m_offset]·2^(-m/2), rounded once from its exact value."""
+    X, Y = counts_to_xy(counts, m_offset)
+    return xy_to_float(X, Y, scale)
 
 
 def seed_bytes(seed) -> np.ndarray | None:
@@ -67,6 +105,20 @@ class QuantumState:
         h = C.c_void_p()
         check(L.nsg_state_from_circuit(num_qubits, _p(rows), len(rows), C.byref(h)))
         return QuantumState(h)
+
+    @staticmethod
+    def from_gates_many(circuits) -> list["QuantumState"]:
+        """Compiles many circuits in one call (nsg_states_from_circuits): ``circuits``
+        is a list of (num_qubits, gates); every compile is queued before any wait."""
+        L = _ffi.load()
+        rows = [gate_rows(g) for _, g in circuits]
+        k = len(rows)
+        nq = np.asarray([int(n) for n, _ in circuits], dtype=np.uint32)
+        ng = np.asarray([len(r) for r in rows], dtype=np.uint64)
+        gp = (C.c_void_p * max(k, 1))(*[r.ctypes.data for r in rows])
+        hs = (C.c_void_p * max(k, 1))()
+        check(L.nsg_states_from_circuits(k, _p(nq), gp, _p(ng), hs))
+        return [QuantumState(C.c_void_p(hs[i])) for i in range(k)]
 
     @staticmethod
     def debug_t_tensor(t: int) -> "QuantumState":
@@ -138,6 +190,31 @@ class QuantumState:
         out = np.zeros(len(paulis), np.float64)
         check(_ffi.load().nsg_exp_value_batch(self._h, arr, len(paulis), precision, _p(out)))
         return out
+
+    def exp_value_counts(self, paulis):
+        """The exact accumulator of ⟨P⟩ for each observable: (counts of shape
+        (nobs, EXACT_BINS) — signed numbers of pair terms with real part
+        2^(-m/2) at index m + EXACT_M_OFFSET — and the scale |g|²)."""
+        paulis = list(paulis)
+        arr = (_ffi.PauliABI * max(len(paulis), 1))()
+        for i, p in enumerate(paulis):
+            arr[i] = p.abi()
+        counts = np.zeros((len(paulis), EXACT_BINS), np.int64)
+        scale = C.c_double()
+        check(_ffi.load().nsg_exp_value_counts(self._h, arr, len(paulis), _p(counts), C.byref(scale)))
+        return counts, scale.value
+
+    def exp_values_exact(self, paulis) -> np.ndarray:
+        """⟨P⟩ rounded once from the exact sum of every pair term."""
+        counts, scale = self.exp_value_counts(paulis)
+        return np.asarray([counts_to_value(c, EXACT_M_OFFSET, scale) for c in counts], np.float64)
+
+    def select(self, indices) -> "QuantumState":
+        """A new state of the terms `indices` (strictly ascending), same global factor."""
+        idx = np.ascontiguousarray(list(indices), dtype=np.uint64)
+        h = C.c_void_p()
+        check(_ffi.load().nsg_state_select(self._h, _p(idx), len(idx), C.byref(h)))
+        return QuantumState(h)
 
     def inner_product(self, other: "QuantumState") -> complex:
         out = np.zeros(2, np.float64)
@@ -251,6 +328,25 @@ class QuantumState:
         keys = ("G", "F", "M", "gamma", "v", "s", "phase", "coef_phase", "coef_r", "coef_zero", "global_factor")
         check(_ffi.load().nsg_export_terms(self._h, *[_p(d[k]) for k in keys]))
         return d
+
+
+def compile_keep(num_qubits: int, gates) -> np.ndarray:
+    """Per term of the T-tensor expansion, whether compilation keeps it (the
+    compiled state's term i is the i-th kept term)."""
+    L = _ffi.load()
+    rows = gate_rows(gates)
+    nt = C.c_uint64()
+    rc = L.nsg_debug_compile_keep(num_qubits, _p(rows), len(rows), None, 0, C.byref(nt))
+    if rc not in (0, 104):
+        check(rc)
+    keep = np.zeros(max(nt.value, 1), np.uint8)
+    check(L.nsg_debug_compile_keep(num_qubits, _p(rows), len(rows), _p(keep), len(keep), C.byref(nt)))
+    return keep[:nt.value].astype(bool)
+
+
+def set_pair_tiling(chunk: int = 0, tasks_per_warp: int = 0) -> None:
+    """Tiling of direct pair sums in this process (0 = default)."""
+    check(_ffi.load().nsg_set_pair_tiling(chunk, tasks_per_warp))
 
 
 def _multi_args(states, paulis_per_state):

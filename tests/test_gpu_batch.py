@@ -20,14 +20,11 @@ def close(a, b, tol=TOL):
 
 
 def oracle_values(oracle, n, gates, paulis):
+    """The oracle's exact ⟨P⟩ (its exact accumulator over the full χ² sum, rows on all host threads)."""
     ref = oracle.OracleState.from_circuit(n, gates)
-    out = []
-    for p in paulis:
-        if p.kind == 0:
-            out.append(ref.exp_value(0, p.ops)[1])
-        else:
-            out.append(ref.exp_value(1, p.ops, p.qubits)[1])
-    return out
+    ops = [(0, p.ops, None) if p.kind == 0 else (1, p.ops, p.qubits) for p in paulis]
+    _, exact = ref.exp_value_counts(ops, 192, 512)
+    return list(exact)
 
 
 # widths on both sides of the 32-bit / 64-bit row boundary, uneven T counts
@@ -103,3 +100,29 @@ def test_multi_argument_checks(gpu_pkg):
     assert gpu_pkg.exp_values_multi([], []) == []
     with pytest.raises(ValueError):
         gpu_pkg.exp_values_multi([a], [])
+
+
+def test_states_from_circuits_equal_single_compiles(gpu_pkg):
+    """The batched compile gives, circuit by circuit, the terms of nsg_state_from_circuit."""
+    circuits = [(n, g) for n, g, _ in W.batch_circuits()[:24]]
+    circuits.append((70, random_full_circuit(70, 300, 5, 41)))  # width 75: two-word rows while compiling
+    many = gpu_pkg.QuantumState.from_gates_many(circuits)
+    assert len(many) == len(circuits)
+    for (n, g), st in zip(circuits, many):
+        one = gpu_pkg.QuantumState.from_gates(n, g)
+        a, b = st.export_terms(), one.export_terms()
+        for k in ("G", "F", "M", "gamma", "v", "s", "phase", "coef_phase", "coef_r"):
+            assert np.array_equal(a[k], b[k]), (n, k)
+    assert gpu_pkg.QuantumState.from_gates_many([]) == []
+
+
+def test_states_from_circuits_reports_the_failing_circuit(gpu_pkg):
+    from stab_decomp_simulator_rust_gb300 import NecstarError
+    good = W.random_clifford_t_circuit(5, 40, 2, 3)
+    bad = np.asarray([[W.OP["CX"], 1, 1, 0]], np.uint32)
+    with pytest.raises(NecstarError) as e:
+        gpu_pkg.QuantumState.from_gates_many([(5, good), (5, good), (5, bad)])
+    assert e.value.code == 14 and e.value.args3[2] == 2
+    with pytest.raises(NecstarError) as e:
+        gpu_pkg.QuantumState.from_gates_many([(5, good), (0, good)])
+    assert e.value.code == 2 and e.value.args3[2] == 1

@@ -2,10 +2,11 @@
 
 Those callers (a process whose GPU memory is fully reserved by another
 allocator, a latency-critical loop where cudaMalloc/cudaFree would
-synchronise the device) get the same value as nsg_exp_value from one static
-16 MiB device scratch array.  This file is collected last so that a run that
-stops at the first failure has already run every other test; it passes both
-alone in a fresh process and after the rest of the suite.
+synchronise the device) get the same value as nsg_exp_value — and, within
+the tolerance of the other expectation-value tests, the oracle's exact sum —
+from one static 16 MiB device scratch array.  This file is collected last so
+that a run that stops at the first failure has already run every other test;
+it passes both alone in a fresh process and after the rest of the suite.
 """
 from __future__ import annotations
 
@@ -28,18 +29,22 @@ def _noalloc(lib, state, pauli):
     return rc, out.value
 
 
-def test_noalloc_matches_exp_value_twice(gpu_pkg):
+def test_noalloc_matches_exp_value_twice(gpu_pkg, oracle):
     from stab_decomp_simulator_rust_gb300 import _ffi
     lib = _ffi.load()
     n = 40
     gates = W.random_clifford_t_circuit(n, 1500, 12, 7)
     st = gpu_pkg.QuantumState.from_gates(n, gates)
-    paulis = [gpu_pkg.PauliString.dense(p) for p in W.random_dense_paulis(n, 2, 70)]
-    for p in paulis:  # two calls in a row share (and reuse) the scratch
+    ref = oracle.OracleState.from_circuit(n, gates)
+    ops = W.random_dense_paulis(n, 2, 70)
+    for o in ops:  # two calls in a row share (and reuse) the scratch
+        p = gpu_pkg.PauliString.dense(o)
         want = st.exp_value(p)
+        _, exact = ref.exp_value(0, o)
         rc, got = _noalloc(lib, st, p)
         assert rc == 0, (rc, lib.nsg_last_error_message())
         assert abs(got - want) <= TOL * max(1.0, abs(want)), (got, want)
+        assert abs(got - exact) <= TOL * max(1.0, abs(exact)), (got, exact)
 
 
 def test_noalloc_small_state_twice(gpu_pkg):
@@ -61,3 +66,42 @@ def test_noalloc_rejects_states_above_its_limit(gpu_pkg):
     rc, _ = _noalloc(lib, st, gpu_pkg.PauliString.from_str("Z0"))
     assert rc == _ffi.header_constants()["NSG_ERR_BUFFER_TOO_SMALL"]
     assert b"8192" in lib.nsg_last_error_message()
+
+
+def test_noalloc_rejects_more_than_64_qubits(gpu_pkg):
+    from stab_decomp_simulator_rust_gb300 import _ffi
+    lib = _ffi.load()
+    st = gpu_pkg.QuantumState.from_gates(65, W.random_clifford_t_circuit(65, 100, 0, 10))
+    rc, _ = _noalloc(lib, st, gpu_pkg.PauliString.from_str("Z0"))
+    assert rc == _ffi.header_constants()["NSG_ERR_TOO_WIDE"]
+
+
+def test_noalloc_after_another_allocator_took_the_memory(gpu_pkg):
+    """The situation the entry point is for: after one call on the device
+    (which loads the library's device code and its scratch array), another
+    allocator reserves nearly all free device memory; calls still succeed."""
+    torch = pytest.importorskip("torch")
+    from stab_decomp_simulator_rust_gb300 import _ffi
+    lib = _ffi.load()
+    st = gpu_pkg.QuantumState.from_gates(16, W.random_clifford_t_circuit(16, 300, 6, 11))
+    p = gpu_pkg.PauliString.from_str("Z1 X4 Y9")
+    rc, want = _noalloc(lib, st, p)  # the first call on this device
+    assert rc == 0, lib.nsg_last_error_message()
+    torch.cuda.synchronize()
+    block = None
+    free, _ = torch.cuda.mem_get_info()
+    for leave in (8 << 20, 32 << 20, 128 << 20):  # keep less free than the 16 MiB scratch if the allocator allows
+        try:
+            block = torch.empty(max(free - leave, 0), dtype=torch.uint8, device="cuda")
+            break
+        except RuntimeError:
+            continue
+    assert block is not None
+    try:
+        for _ in range(2):
+            rc, got = _noalloc(lib, st, p)
+            assert rc == 0, (rc, lib.nsg_last_error_message())
+            assert got == want
+    finally:
+        del block
+        torch.cuda.empty_cache()
