@@ -32,10 +32,10 @@ step over Σχ(χ+1)/2 ≈ 1.04·10⁹ term pairs.
   64 dense Paulis) as a second line item.
 * ``cpu_baseline`` / ``--impl reference``: the C++ restatement of the
   reference's Rust path (the reference cannot be built here: no Rust
-  toolchain) on the host cores: per step one circuit drawn from the 512
-  (probability half by pair count, half uniform), compiled with the
-  reference's compile loop and timed on a uniform sample of its term pairs;
-  the whole workload's time is the Horvitz-Thompson estimate over the steps.
+  toolchain) on the host cores: per step one circuit drawn from the 512 in
+  proportion to its expected cost, compiled with the reference's compile loop
+  and timed on a uniform sample of its term pairs; the whole workload's time
+  is the Horvitz-Thompson estimate over the steps.
 
 Other workloads (one JSON line each): --workload plain40 | precision60 |
 project64 | gates.
@@ -145,19 +145,23 @@ def oracle_batch_estimate(circuits, steps: int, step_pair_seconds: float, thread
                           single_thread: bool = False):
     """Times the reference algorithm on the batching workload, one sampled circuit per step.
 
-    Step k draws circuit c with probability q_c = ½·P_c/ΣP + ½/N (P_c: the pair
-    count of its T-expansion size), compiles it with the reference's compile
-    loop on all `threads`, and times a uniform sample of its term pairs (one
-    of its observables, the reference inner-product algorithm) for about
-    `step_pair_seconds`.  The workload's time is the Horvitz-Thompson
-    estimate mean_k[(compile_k + 16·pairs_k·sec_per_pair_k) / q_k]."""
+    Step k draws circuit c with probability q_c ∝ P_c·n_c³ (P_c: the pair
+    count of its T-expansion size, an upper bound of its compiled pair count;
+    the reference's per-pair cost grows about as n³), compiles it with the
+    reference's compile loop on all `threads`, and times a uniform sample of
+    its term pairs (one of its observables, the reference inner-product
+    algorithm) for about `step_pair_seconds`.  The workload's time is the
+    Horvitz-Thompson estimate mean_k[(compile_k + 16·pairs_k·sec_per_pair_k)
+    / q_k]: draws in proportion to the expected cost keep its spread small,
+    since the pair evaluations are nearly all of the time."""
     from oracle import pyoracle as po
     N = len(circuits)
     nobs = sum(len(ps) for _, _, ps in circuits)
     tcount = [int((np.asarray(g)[:, 0] == 11).sum() + (np.asarray(g)[:, 0] == 12).sum()) for _, g, _ in circuits]
     chiT = np.asarray([po.t_tensor_rank(t) if t else 1 for t in tcount], dtype=np.float64)
     P = chiT * (chiT + 1) / 2
-    q = 0.5 * P / P.sum() + 0.5 / N
+    nq = np.asarray([n for n, _, _ in circuits], dtype=np.float64)
+    q = P * nq ** 3 / (P * nq ** 3).sum()
     rng = np.random.default_rng(seed)
     est, step_ms, draws = [], [], []
     last = None
@@ -183,7 +187,7 @@ def oracle_batch_estimate(circuits, steps: int, step_pair_seconds: float, thread
     total_s = float(np.mean(est))
     stderr_s = float(np.std(est, ddof=1) / np.sqrt(len(est))) if len(est) > 1 else None
     out = {"value": nobs / total_s, "unit": UNIT, "cores": threads, "kind": "port",
-           "sample": (f"{steps} circuits drawn from the 512 (probability half by pair count, half uniform); each "
+           "sample": (f"{steps} circuits drawn from the 512 in proportion to pairs x n^3 (their expected cost); each "
                       f"compiled with the reference compile loop on {threads} threads and timed on a uniform sample "
                       f"of ~{step_pair_seconds:.1f} s of its term pairs (reference inner-product algorithm); the "
                       f"{nobs} <P> of all 512 circuits extrapolated by the Horvitz-Thompson estimate"),

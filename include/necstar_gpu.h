@@ -225,9 +225,10 @@ nsg_status nsg_exp_value_counts(const nsg_state* state, const nsg_pauli* paulis,
                                 int64_t* counts, double* scale);
 
 /* Tiling of the direct (uncaptured) pair sums of this process: kets per
- * chunk and tasks per resident warp of the persistent pair launch; 0 keeps
- * the default (32 and 8).  Results do not depend on it beyond FP rounding
- * of the partial sums (no reference counterpart). */
+ * chunk and tasks per resident warp of the persistent pair launch; 0 takes
+ * the tuned choice of the workload class if a plan tuned one, else the
+ * default (32 and 8).  Results do not depend on it beyond FP rounding of the
+ * partial sums (no reference counterpart). */
 nsg_status nsg_set_pair_tiling(int32_t chunk, int32_t tasks_per_warp);
 
 /* ⟨P⟩ for callers that cannot allocate device memory at call time — a
@@ -255,19 +256,23 @@ nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pauli* pauli,
  * gates applied in place (nsg_apply_gates) are seen by the next run; an
  * operation that changes a state's rank, width or global factor (projection,
  * discard, measurement) or frees it makes nsg_plan_run fail with
- * NSG_ERR_INVALID_ARGUMENT.  Creation picks the pair-kernel variant for each
- * row width by timing the candidates on the plan's own work (whole launches
- * when short, else the first two tasks per resident warp), remembered per
- * device and workload class for the process; when the environment variable NSG_TUNE_CACHE names a file, the
- * choices are also read from and appended to it (one JSON object per line). */
+ * NSG_ERR_INVALID_ARGUMENT.  Creation picks, for each row width, the
+ * pair-kernel variant (2-5 blocks per SM), the tasks per resident warp (4, 8,
+ * 16) and the kets per chunk (16, 32, 64), in that order, by timing the
+ * candidates on the plan's own work (whole launches when short, else the
+ * first two tasks per resident warp); the choice is remembered per device
+ * and workload class for the process (direct calls of the same class use it
+ * too) and, when the environment variable NSG_TUNE_CACHE names a file, read
+ * from and appended to it (one JSON object per line). */
 typedef struct nsg_plan nsg_plan;
 nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, const nsg_pauli* paulis,
                            const uint64_t* pauli_offsets, uint32_t precision, nsg_plan** out);
 nsg_status nsg_plan_run(nsg_plan* plan, double* out);
-/* The tiling in use: kets per chunk, tasks per resident warp, the kernel
- * variant (blocks per SM its registers allow) for 32- and 64-bit rows, and
- * whether creation timed candidates (1) or took them from the cache (0). */
-nsg_status nsg_plan_info(const nsg_plan* plan, int32_t* chunk, int32_t* tasks_per_warp, int32_t minb[2],
+/* The tiling in use for 32-bit ([0]) and 64-bit ([1]) rows: kets per chunk,
+ * tasks per resident warp, the kernel variant (blocks per SM its registers
+ * allow); 0 where the plan has no launch of that width.  *timed = 1 when
+ * creation timed candidates, 0 when it took them from the cache. */
+nsg_status nsg_plan_info(const nsg_plan* plan, int32_t chunk[2], int32_t tasks_per_warp[2], int32_t minb[2],
                          int32_t* timed);
 void nsg_plan_free(nsg_plan* plan);
 
@@ -329,6 +334,17 @@ nsg_status nsg_to_statevector(const nsg_state* state, double* out, size_t capaci
  * global factors multiply (the reference's result has factor 1, which is the
  * product wherever it calls it).  Both states must be on one device. */
 nsg_status nsg_state_kron(const nsg_state* a, const nsg_state* b, nsg_state** out);
+
+/* |Toffoli⟩^{⊗k} = ((|000⟩ + |100⟩ + |010⟩ + |111⟩)/2)^{⊗k} as a state of
+ * 3k qubits and 2^k terms, in the order of construct_toffoli_tensor_state
+ * (crates/necstar/src/state/magic_states/toffoli_state.rs:12-40: the
+ * two-term |0+0⟩, |1⟩⊗Bell decomposition, each term 2^{-1/2}, joined by
+ * kron): the base state is built on the host and the joins run on the
+ * device (nsg_state_kron).  1 ≤ k ≤ 21 (n ≤ 63): k = 0 gives
+ * NSG_ERR_INVALID_NUM_QUBITS, larger k NSG_ERR_TOO_WIDE.  The reference
+ * marks the construction crate-internal and unused (Toffoli-state injection
+ * is not implemented there either). */
+nsg_status nsg_toffoli_tensor_state(uint32_t num_tensors, nsg_state** out);
 
 /* QuantumCircuit::random_clifford (crates/necstar/src/circuit/mod.rs:289-291
  * → crates/stabilizer-ch-form-rust/src/circuit/random_clifford.rs:177-212):

@@ -908,6 +908,23 @@ static std::pair<ChForm, Scalar> t_tensor_term(int nq, int64_t k) {
     return {c.first, coef};
 }
 
+// construct_toffoli_state / construct_toffoli_tensor_state
+// (crates/necstar/src/state/magic_states/toffoli_state.rs:12-40).
+static SDState construct_toffoli() {
+    ChForm a = ch_new(3);  // |0+0⟩
+    left_h(a, 1);
+    ChForm b = ch_new(3);  // |1⟩⊗Bell
+    left_x(b, 0);
+    left_h(b, 1);
+    left_cx(b, 1, 2);
+    return mk_sd(3, {a, b}, {S_ONE_OVER_SQRT2, S_ONE_OVER_SQRT2});
+}
+static SDState construct_toffoli_tensor(int k) {
+    if (k == 0) fail(NSG_ERR_INVALID_NUM_QUBITS, 0);
+    if (k == 1) return construct_toffoli();
+    return sd_kron(construct_toffoli_tensor(k - 1), construct_toffoli());
+}
+
 // ---------------------------------------------------------------------------
 // Compiler (crates/necstar/src/state/compiler/mod.rs:44-140)
 static bool is_clifford_op(uint32_t op) { return op <= NSG_GATE_SWAP; }
@@ -1704,6 +1721,12 @@ int orc_t_tensor_terms(uint32_t t, const int64_t* tidx, size_t count, void** out
         st->coeffs.push_back(tt.second);
     }
     *out = st;
+    ORC_CATCH
+}
+
+int orc_toffoli_tensor_state(uint32_t k, void** out) {
+    ORC_TRY
+    *out = new SDState(construct_toffoli_tensor((int)k));
     ORC_CATCH
 }
 

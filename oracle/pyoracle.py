@@ -77,6 +77,7 @@ def lib():
                                      C.POINTER(C.c_double), C.POINTER(C.c_double)]
         L.orc_t_tensor_terms.argtypes = [C.c_uint32, C.c_void_p, C.c_size_t, C.POINTER(vp)]
         L.orc_t_tensor_rank.argtypes = [C.c_uint32, C.POINTER(C.c_uint64)]
+        L.orc_toffoli_tensor_state.argtypes = [C.c_uint32, C.POINTER(vp)]
         L.orc_compile_terms.argtypes = [C.c_uint32, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_int32,
                                         C.c_void_p, C.POINTER(vp)]
         L.orc_exp_value_counts.argtypes = [vp, C.POINTER(PauliABI), C.c_size_t, C.c_int32, C.c_int64, C.c_int64,
@@ -137,6 +138,13 @@ class OracleState:
     def t_tensor(t: int) -> "OracleState":
         h = C.c_void_p()
         _check(lib().orc_t_tensor_state(t, C.byref(h)))
+        return OracleState(h)
+
+    @staticmethod
+    def toffoli_tensor(k: int) -> "OracleState":
+        """construct_toffoli_tensor_state (magic_states/toffoli_state.rs:12-40)."""
+        h = C.c_void_p()
+        _check(lib().orc_toffoli_tensor_state(k, C.byref(h)))
         return OracleState(h)
 
     @staticmethod

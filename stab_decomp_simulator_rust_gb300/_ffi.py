@@ -68,7 +68,7 @@ def load(path: str | None = None):
     L.nsg_exp_value_multi.argtypes = [vp, sz, P(PauliABI), vp, u32, vp]
     L.nsg_plan_create.argtypes = [vp, sz, P(PauliABI), vp, u32, P(vp)]
     L.nsg_plan_run.argtypes = [vp, vp]
-    L.nsg_plan_info.argtypes = [vp, P(i32), P(i32), vp, P(i32)]
+    L.nsg_plan_info.argtypes = [vp, vp, vp, vp, P(i32)]
     L.nsg_plan_free.argtypes = [vp]
     L.nsg_plan_free.restype = None
     L.nsg_inner_product.argtypes = [vp, vp, vp]
@@ -96,6 +96,7 @@ def load(path: str | None = None):
     L.nsg_state_select.argtypes = [vp, vp, sz, P(vp)]
     L.nsg_debug_set_wait.argtypes = [u32, u32]
     L.nsg_states_from_circuits.argtypes = [sz, vp, vp, vp, vp]
+    L.nsg_toffoli_tensor_state.argtypes = [u32, P(vp)]
     for name in header_symbols():
         fn = getattr(L, name)
         if name not in ("nsg_version", "nsg_last_error_message", "nsg_state_free", "nsg_plan_free"):

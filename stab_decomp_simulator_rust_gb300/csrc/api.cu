@@ -626,13 +626,20 @@ struct UnitSources {
 };
 
 // ---- tuning of captured batches ----------------------------------------------
-// The kernel variant (blocks per SM its registers allow) that ran fastest on a
-// sample, per device and workload class; also appended to the file named by
-// NSG_TUNE_CACHE, one JSON object per line: {"key": "...", "minb": k}.
+// The tiling of one row width that ran fastest on a sample, per device and
+// workload class: kernel variant (blocks per SM its registers allow), tasks
+// per resident warp and kets per chunk.  Also appended to the file named by
+// NSG_TUNE_CACHE, one JSON object per line:
+// {"key": "...", "minb": k, "tasks_per_warp": t, "chunk": c}.
+struct TuneChoice {
+    int minb = 0, tasks_per_warp = 8, chunk = 32;
+};
 std::mutex g_tune_mu;
-std::map<std::string, int> g_tune;
+std::map<std::string, TuneChoice> g_tune;
 bool g_tune_loaded = false;
 constexpr int kMinbCandidates[4] = {2, 3, 4, 5};
+constexpr int kTpwCandidates[3] = {4, 8, 16};
+constexpr int kChunkCandidates[3] = {16, 32, 64};
 
 // Device names by ordinal (cudaGetDeviceProperties is slow; asked once per device).
 std::string device_name(int device) {
@@ -670,30 +677,34 @@ void tune_load_locked() {
     char line[512];
     while (std::fgets(line, sizeof(line), f)) {
         char key[256];
-        int minb = 0;
-        if (std::sscanf(line, " {\"key\": \"%255[^\"]\", \"minb\": %d}", key, &minb) == 2 && minb >= 2 && minb <= 5)
-            g_tune[key] = minb;
+        TuneChoice c;
+        const int got = std::sscanf(line, " {\"key\": \"%255[^\"]\", \"minb\": %d, \"tasks_per_warp\": %d, \"chunk\": %d}",
+                                    key, &c.minb, &c.tasks_per_warp, &c.chunk);
+        if (got >= 2 && c.minb >= 2 && c.minb <= 5 && c.tasks_per_warp >= 1 && c.tasks_per_warp <= 1024 &&
+            c.chunk >= 1 && c.chunk <= 1024)
+            g_tune[key] = c;  // a line without the last two fields keeps their defaults
     }
     std::fclose(f);
 }
 
-bool tune_lookup(const std::string& key, int& minb) {
+bool tune_lookup(const std::string& key, TuneChoice& c) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     tune_load_locked();
     auto it = g_tune.find(key);
     if (it == g_tune.end()) return false;
-    minb = it->second;
+    c = it->second;
     return true;
 }
 
-void tune_store(const std::string& key, int minb) {
+void tune_store(const std::string& key, const TuneChoice& c) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     tune_load_locked();
-    g_tune[key] = minb;
+    g_tune[key] = c;
     const char* path = std::getenv("NSG_TUNE_CACHE");
     if (!path || !*path) return;
     if (FILE* f = std::fopen(path, "a")) {
-        std::fprintf(f, "{\"key\": \"%s\", \"minb\": %d}\n", key.c_str(), minb);
+        std::fprintf(f, "{\"key\": \"%s\", \"minb\": %d, \"tasks_per_warp\": %d, \"chunk\": %d}\n", key.c_str(),
+                     c.minb, c.tasks_per_warp, c.chunk);
         std::fclose(f);
     }
 }
@@ -709,12 +720,14 @@ int default_minb(int wb, int nobs_max, int n_mean) {
     return nobs_max > 128 ? 2 : 3;
 }
 
-// Tiling of a pair launch: kets per chunk, tasks per resident warp, and the
-// kernel variant (blocks per SM its registers allow) for 32- and 64-bit rows;
-// 0 = the tuning cache's choice for the workload class, else default_minb.
+// Tiling of a pair launch, per row width ([0] 32-bit, [1] 64-bit rows): kets
+// per chunk, tasks per resident warp and the kernel variant (blocks per SM its
+// registers allow).  0 = the tuning cache's choice for the workload class,
+// else the defaults: 32 kets, 8 tasks per warp (2, 4, 8 measured on n = 28,
+// 40, 60: 8 fastest, balance at the end of the queue), default_minb.
 struct PairTiling {
-    int chunk = 32;
-    int tasks_per_warp = 8;  // 2, 4, 8 measured on n = 28, 40, 60: 8 fastest (balance at the end of the queue)
+    int chunk[2] = {0, 0};
+    int tasks_per_warp[2] = {0, 0};
     int minb[2] = {0, 0};
 };
 
@@ -745,6 +758,7 @@ struct PairBatch {
         int64_t pairs_total = 0;          // pairs of the whole launch
         size_t rec_used = 0;              // doubles of `rec` to clear before a launch (records, counter)
         double* red_scratch = nullptr;    // partials of the two-pass reduction
+        int chunk = 32, tpw = 8, minb = 4;  // the tiling the launch was built with
     };
     std::vector<PairUnit*> live;
     std::vector<UnitSources> src;
@@ -805,6 +819,31 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
         std::vector<size_t> off_at(sel.size(), 0);
         size_t tab_max = 0, bra_max = 0;
         int nobs_max = 1;
+        for (size_t q = 0; q < sel.size(); q++) nobs_max = std::max(nobs_max, b.live[sel[q]]->nobs);
+        // The tiling of this row width: as given, else the tuning cache's choice
+        // for the workload class, else the defaults.
+        const int widx = wb == 4 ? 0 : 1;
+        int chunk = tl.chunk[widx], tpw = tl.tasks_per_warp[widx];
+        int minb = exact ? -1 : tl.minb[widx];
+        if (minb == 0 || chunk == 0 || tpw == 0) {
+            uint64_t pairs = 0, nsum = 0;
+            for (size_t q = 0; q < sel.size(); q++) {
+                const int64_t chi = b.live[sel[q]]->a->t.chi;
+                pairs += (uint64_t)(chi * (chi + 1) / 2);
+                nsum += (uint64_t)b.live[sel[q]]->a->t.n * (uint64_t)(chi * (chi + 1) / 2);
+            }
+            int dev = 0;
+            CK(cudaGetDevice(&dev));
+            const int n_mean = pairs ? (int)(nsum / pairs) : 0;
+            TuneChoice c;
+            const bool hit = tune_lookup(tune_key(dev, wb, nobs_max, n_mean, pairs), c);
+            if (minb == 0) minb = hit ? c.minb : default_minb(wb, nobs_max, n_mean);
+            if (tpw == 0) tpw = hit ? c.tasks_per_warp : TuneChoice().tasks_per_warp;
+            if (chunk == 0) chunk = hit ? c.chunk : TuneChoice().chunk;
+        }
+        ln.chunk = chunk;
+        ln.tpw = tpw;
+        ln.minb = minb;
         for (size_t q = 0; q < sel.size(); q++) {
             PairUnit* u = b.live[sel[q]];
             const UnitSources& s = b.src[sel[q]];
@@ -838,13 +877,13 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
                 int64_t acc = 0;
                 for (int64_t i = 0; i < chiA; i++) {
                     offs.push_back(acc);
-                    acc += (chiA - i + tl.chunk - 1) / tl.chunk;
+                    acc += (chiA - i + chunk - 1) / chunk;
                 }
                 offs.push_back(acc);
                 nch = acc;
                 b.pairs += (uint64_t)(chiA * (chiA + 1) / 2);
             } else {
-                d.cpr = (chiB + tl.chunk - 1) / tl.chunk;
+                d.cpr = (chiB + chunk - 1) / chunk;
                 nch = chiA * d.cpr;
                 b.pairs += (uint64_t)(chiA * chiB);
             }
@@ -853,7 +892,6 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
             b.unit_out[sel[q]] = out_base + (size_t)ln.obegin[q];
             tab_max = std::max(tab_max, (size_t)d.ket_bytes);
             bra_max = std::max(bra_max, ket_table_bra_bytes(u->b->t.n));
-            nobs_max = std::max(nobs_max, u->nobs);
         }
         out_base += (size_t)ln.obegin.back();
         for (const PairDesc& d : descs)  // imaginary parts are accumulated with one observable group only
@@ -861,23 +899,10 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
                 raise(NSG_ERR_INVALID_ARGUMENT, nobs_max, 32, "complex pair sums take at most 32 observables per launch");
         // Tasks: about tasks_per_warp per resident warp, never spanning two units.
         const size_t warp_smem = pair_warp_smem_bytes(tab_max, bra_max, wb);
-        int minb = exact ? -1 : tl.minb[wb == 4 ? 0 : 1];
-        if (minb == 0) {
-            uint64_t pairs = 0, nsum = 0;
-            for (size_t q = 0; q < sel.size(); q++) {
-                const int64_t chi = b.live[sel[q]]->a->t.chi;
-                pairs += (uint64_t)(chi * (chi + 1) / 2);
-                nsum += (uint64_t)b.live[sel[q]]->a->t.n * (uint64_t)(chi * (chi + 1) / 2);
-            }
-            int dev = 0;
-            CK(cudaGetDevice(&dev));
-            const int n_mean = pairs ? (int)(nsum / pairs) : 0;
-            if (!tune_lookup(tune_key(dev, wb, nobs_max, n_mean, pairs), minb)) minb = default_minb(wb, nobs_max, n_mean);
-        }
         const int64_t resident = pair_resident_warps(wb, nobs_max, warp_smem, exact ? 0 : minb);
         int64_t total_chunks = 0;
         for (const PairDesc& d : descs) total_chunks += d.nchunks;
-        const int64_t want = (int64_t)tl.tasks_per_warp * resident;
+        const int64_t want = (int64_t)tpw * resident;
         const int64_t task_chunks = std::max<int64_t>(1, (total_chunks + want - 1) / want);
         int64_t rec_doubles = 0;
         for (size_t q = 0; q < sel.size(); q++) {
@@ -894,16 +919,16 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
                 const PairUnit* u = b.live[sel[q]];
                 const int64_t chiA = u->a->t.chi, chiB = u->b->t.chi;
                 if (!u->triangular)
-                    return (c / descs[q].cpr) * chiB + std::min<int64_t>((c % descs[q].cpr) * tl.chunk, chiB);
+                    return (c / descs[q].cpr) * chiB + std::min<int64_t>((c % descs[q].cpr) * chunk, chiB);
                 const int64_t* off = offs.data() + off_at[q];
                 const int64_t i = (int64_t)(std::upper_bound(off, off + chiA + 1, c) - off) - 1;
                 if (i >= chiA) return chiA * (chiA + 1) / 2;
-                return i * chiA - i * (i - 1) / 2 + std::min<int64_t>((c - off[i]) * tl.chunk, chiA - i);
+                return i * chiA - i * (i - 1) / 2 + std::min<int64_t>((c - off[i]) * chunk, chiA - i);
             };
             ln.pairs_total = 0;
             for (size_t q = 0; q < sel.size(); q++) ln.pairs_total += pairs_before(q, descs[q].nchunks);
             const int64_t lim =
-                with_samples ? std::min<int64_t>(total_tasks, 2 * (int64_t)tl.tasks_per_warp * resident) : 0;
+                with_samples ? std::min<int64_t>(total_tasks, 2 * (int64_t)tpw * resident) : 0;
             ln.task_pairs.assign((size_t)lim + 1, 0);
             int64_t before = 0;  // pairs of the units before q
             size_t q = 0;
@@ -940,7 +965,7 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
         m.task_begin = d_db;
         m.total_tasks = total_tasks;
         m.task_chunks = (int)task_chunks;
-        m.chunk = tl.chunk;
+        m.chunk = chunk;
         m.nobs_max = nobs_max;
         m.mixed = mixed;
         m.exact = exact;
@@ -1393,10 +1418,15 @@ namespace {
 // phases so that many circuits can be enqueued before any host wait:
 // compile_enqueue lowers the circuit (with the reference's checks, in its
 // order), creates the state and queues the compile kernel and the stable
-// compaction of the kept terms on the state's stream; compile_finish waits for
-// that stream and installs the compacted terms.
+// compaction of the kept terms; compile_finish waits for that work and
+// installs the compacted terms.  A batch queues everything on one work
+// stream: the allocator then reuses freed memory in stream order instead of
+// searching blocks freed on hundreds of other streams (measured: 11 s instead
+// of 1.1 s for the second batch of 512 circuits when every state used its own
+// stream); the buffers move to each state's own stream when it is finished.
 struct PendingCompile {
     std::unique_ptr<nsg_state> s;
+    cudaStream_t ws = nullptr;   // the stream the work is queued on (the state's own when null)
     TermStore out;               // the compaction's target
     DBuf<int32_t> keep, pos;
     DBuf<int64_t> cnt;
@@ -1405,7 +1435,8 @@ struct PendingCompile {
     int64_t* h_count = nullptr;  // pinned slot the kept count is copied to
 };
 
-void compile_enqueue(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates, PendingCompile& pc) {
+void compile_enqueue(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates, PendingCompile& pc,
+                     cudaStream_t work = nullptr) {
     if (num_gates) need(gates, "gates");
     const int n = (int)num_qubits;
     // Lowering (compiler/mod.rs:49-63): T/Tdg -> CX(target, n+k) [+ Sdg(target)].
@@ -1442,6 +1473,11 @@ void compile_enqueue(uint32_t num_qubits, const nsg_gate* gates, size_t num_gate
     nsg_state* s = pc.s.get();
     s->init_stream();
     cudaStream_t st = s->st;
+    if (work) {
+        join_stream(work, s->st);  // the status words are cleared on the state's stream
+        st = work;
+    }
+    pc.ws = st;
     auto tt = t_tensor_dev(t, st, s->status.p);
     pc.chi_t = tt->chi;
     pc.dops.alloc(std::max<size_t>(ops.size(), 1), st);
@@ -1465,17 +1501,18 @@ void compile_enqueue(uint32_t num_qubits, const nsg_gate* gates, size_t num_gate
 
 void compile_finish(PendingCompile& pc, std::vector<uint8_t>* keep_out) {
     nsg_state* s = pc.s.get();
-    CK(cudaStreamSynchronize(s->st));
+    CK(cudaStreamSynchronize(pc.ws));
     s->check_status();
     if (keep_out) {
         std::vector<int32_t> hk((size_t)pc.chi_t);
-        CK(cudaMemcpyAsync(hk.data(), pc.keep.p, hk.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
-        CK(cudaStreamSynchronize(s->st));
+        CK(cudaMemcpyAsync(hk.data(), pc.keep.p, hk.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, pc.ws));
+        CK(cudaStreamSynchronize(pc.ws));
         keep_out->assign(hk.size(), 0);
         for (size_t i = 0; i < hk.size(); i++) (*keep_out)[i] = hk[i] ? 1 : 0;
     }
     pc.out.chi = *pc.h_count;
-    s->t = std::move(pc.out);
+    s->t = std::move(pc.out);  // the uncompacted terms are freed on the work stream
+    s->t.rehome(s->st);        // from now on the state's own stream uses (and frees) its terms
     s->layout_gen++;
     s->invalidate();
     pc.keep.release();
@@ -1523,14 +1560,21 @@ nsg_status nsg_states_from_circuits(size_t num_circuits, const uint32_t* num_qub
     }
     for (size_t c = 0; c < num_circuits; c++) out[c] = nullptr;
     PinnedCounts counts(num_circuits);
+    struct WorkStream {
+        cudaStream_t st = nullptr;
+        ~WorkStream() {
+            if (st) cudaStreamDestroy(st);  // destroyed once its queued work (frees included) is done
+        }
+    } work;
+    CK(cudaStreamCreateWithFlags(&work.st, cudaStreamNonBlocking));
     std::vector<PendingCompile> pend(num_circuits);
     for (size_t c = 0; c < num_circuits; c++) {
         pend[c].h_count = counts.p + c;
         try {
-            compile_enqueue(num_qubits[c], gates[c], num_gates[c], pend[c]);
+            compile_enqueue(num_qubits[c], gates[c], num_gates[c], pend[c], work.st);
         } catch (const ApiError& e) {
             g_args[2] = (int64_t)c;  // the failing circuit
-            for (size_t j = 0; j < c; j++) CK(cudaStreamSynchronize(pend[j].s->st));
+            CK(cudaStreamSynchronize(work.st));
             throw;
         }
     }
@@ -1539,7 +1583,7 @@ nsg_status nsg_states_from_circuits(size_t num_circuits, const uint32_t* num_qub
             compile_finish(pend[c], nullptr);
         } catch (const ApiError& e) {
             g_args[2] = (int64_t)c;
-            for (size_t j = c + 1; j < num_circuits; j++) CK(cudaStreamSynchronize(pend[j].s->st));
+            CK(cudaStreamSynchronize(work.st));
             throw;
         }
     }
@@ -1841,9 +1885,10 @@ nsg_status nsg_set_pair_tiling(int32_t chunk, int32_t tasks_per_warp) {
     if (chunk < 0 || chunk > 1024 || tasks_per_warp < 0 || tasks_per_warp > 1024)
         raise(NSG_ERR_INVALID_ARGUMENT, chunk, tasks_per_warp, "tiling out of range");
     std::lock_guard<std::mutex> lk(g_tiling_mu);
-    const PairTiling def;
-    g_tiling_override.chunk = chunk ? chunk : def.chunk;
-    g_tiling_override.tasks_per_warp = tasks_per_warp ? tasks_per_warp : def.tasks_per_warp;
+    for (int w = 0; w < 2; w++) {
+        g_tiling_override.chunk[w] = chunk;  // 0: the tuning cache's choice, else the default
+        g_tiling_override.tasks_per_warp[w] = tasks_per_warp;
+    }
     API_END
 }
 
@@ -1922,11 +1967,20 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
     }
     plan->enqueue_derived();
 
-    // Tiling: the kernel variant per row width, from the cache or timed on a sample.
+    // Tiling per row width — kernel variant, tasks per resident warp, kets per
+    // chunk — from the cache, or timed on the plan's own work: the variants
+    // first (default tasks and chunk), then tasks per warp with the fastest
+    // variant, then the chunk length with both.
     PairTiling tl;
     {
         PairBatch probe;
-        plan->build(probe, tl, mixed, true);
+        PairTiling none;
+        for (int w = 0; w < 2; w++) {
+            none.chunk[w] = TuneChoice().chunk;
+            none.tasks_per_warp[w] = TuneChoice().tasks_per_warp;
+            none.minb[w] = 4;
+        }
+        plan->build(probe, none, mixed, true);
         std::vector<std::string> keys(2);
         bool need_time[2] = {false, false};
         for (const PairBatch::Launch& ln : probe.launches) {
@@ -1938,9 +1992,14 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
                 nsum += (uint64_t)probe.live[q]->a->t.n * (uint64_t)(chi * (chi + 1) / 2);
             }
             keys[idx] = tune_key(plan->device, ln.wb, ln.m.nobs_max, pairs ? (int)(nsum / pairs) : 0, pairs);
-            int minb = 4;
-            if (tune_lookup(keys[idx], minb)) tl.minb[idx] = minb;
-            else need_time[idx] = true;
+            TuneChoice c;
+            if (tune_lookup(keys[idx], c)) {
+                tl.minb[idx] = c.minb;
+                tl.tasks_per_warp[idx] = c.tasks_per_warp;
+                tl.chunk[idx] = c.chunk;
+            } else {
+                need_time[idx] = true;
+            }
         }
         if (need_time[0] || need_time[1]) {
             plan->timed = true;
@@ -1960,38 +2019,72 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
                 const double frac = (double)std::min<int64_t>(m.total_tasks, 2 * (int64_t)m.nwarps) / (double)m.total_tasks;
                 if (ms / frac < 40.0) rounds[idx] = 0;
             }
-            double best[2] = {1e300, 1e300};
-            int pick[2] = {tl.minb[0], tl.minb[1]};
-            for (int cand : kMinbCandidates) {
-                PairTiling tc = tl;
-                for (int idx = 0; idx < 2; idx++)
-                    if (need_time[idx]) tc.minb[idx] = cand;
-                PairBatch b;
-                plan->build(b, tc, mixed, true);
-                for (size_t k = 0; k < b.live.size(); k++)
-                    CK(launch_pauli_frames(b.live[k]->a->t.view(), b.dp.p + b.unit_obs[k], b.live[k]->nobs,
-                                           b.px.p + b.unit_px[k], b.pk.p + b.unit_px[k], st));
-                for (size_t li = 0; li < b.launches.size(); li++) {
-                    const int idx = b.launches[li].wb == 4 ? 0 : 1;
-                    if (!need_time[idx]) continue;
-                    sample_ns_per_pair(b, li, st, 1);  // first launch of the variant: warm-up
-                    const double ns = sample_ns_per_pair(b, li, st, rounds[idx]);
-                    if (ns < best[idx]) {
-                        best[idx] = ns;
-                        pick[idx] = cand;
+            TuneChoice best[2];
+            double best_ns[2] = {1e300, 1e300};
+            for (int w = 0; w < 2; w++) best[w] = TuneChoice();
+            // one stage: time the candidates `vals` of one field (the others at their best so far)
+            auto stage = [&](int field, const int* vals, int nvals) {
+                for (int v = 0; v < nvals; v++) {
+                    PairTiling tc = tl;
+                    bool any = false;
+                    for (int idx = 0; idx < 2; idx++) {
+                        if (!need_time[idx]) continue;
+                        TuneChoice c = best[idx];
+                        if (c.minb == 0) c.minb = 4;
+                        if (field == 0) c.minb = vals[v];
+                        if (field == 1) c.tasks_per_warp = vals[v];
+                        if (field == 2) c.chunk = vals[v];
+                        tc.minb[idx] = c.minb;
+                        tc.tasks_per_warp[idx] = c.tasks_per_warp;
+                        tc.chunk[idx] = c.chunk;
+                        any = true;
                     }
+                    if (!any) return;
+                    PairBatch b;
+                    plan->build(b, tc, mixed, true);
+                    for (size_t k = 0; k < b.live.size(); k++)
+                        CK(launch_pauli_frames(b.live[k]->a->t.view(), b.dp.p + b.unit_obs[k], b.live[k]->nobs,
+                                               b.px.p + b.unit_px[k], b.pk.p + b.unit_px[k], st));
+                    for (size_t li = 0; li < b.launches.size(); li++) {
+                        const int idx = b.launches[li].wb == 4 ? 0 : 1;
+                        if (!need_time[idx]) continue;
+                        sample_ns_per_pair(b, li, st, 1);  // first launch of the candidate: warm-up
+                        const double ns = sample_ns_per_pair(b, li, st, rounds[idx]);
+                        if (ns < best_ns[idx]) {
+                            best_ns[idx] = ns;
+                            best[idx].minb = tc.minb[idx];
+                            best[idx].tasks_per_warp = tc.tasks_per_warp[idx];
+                            best[idx].chunk = tc.chunk[idx];
+                        }
+                    }
+                    CK(cudaStreamSynchronize(st));
                 }
-                CK(cudaStreamSynchronize(st));
-            }
+                for (int idx = 0; idx < 2; idx++)
+                    if (need_time[idx]) {
+                        tl.minb[idx] = best[idx].minb;
+                        tl.tasks_per_warp[idx] = best[idx].tasks_per_warp;
+                        tl.chunk[idx] = best[idx].chunk;
+                    }
+            };
             for (int idx = 0; idx < 2; idx++)
                 if (need_time[idx]) {
-                    tl.minb[idx] = pick[idx];
-                    tune_store(keys[idx], pick[idx]);
+                    tl.tasks_per_warp[idx] = TuneChoice().tasks_per_warp;
+                    tl.chunk[idx] = TuneChoice().chunk;
                 }
+            stage(0, kMinbCandidates, 4);
+            stage(1, kTpwCandidates, 3);
+            stage(2, kChunkCandidates, 3);
+            for (int idx = 0; idx < 2; idx++)
+                if (need_time[idx]) tune_store(keys[idx], best[idx]);
         }
     }
-    plan->tiling = tl;
     plan->build(plan->batch, tl, mixed);
+    for (const PairBatch::Launch& ln : plan->batch.launches) {  // the tiling each launch was built with
+        const int idx = ln.wb == 4 ? 0 : 1;
+        plan->tiling.chunk[idx] = ln.chunk;
+        plan->tiling.tasks_per_warp[idx] = ln.tpw;
+        plan->tiling.minb[idx] = ln.minb;
+    }
     const size_t nres = 2 * std::max<size_t>(plan->batch.tot_obs, 1);
     CK(cudaMallocHost(&plan->pinned, nres * sizeof(double)));
     if (!plan->batch.live.empty()) {
@@ -2034,12 +2127,14 @@ nsg_status nsg_plan_run(nsg_plan* plan, double* out) {
     API_END
 }
 
-nsg_status nsg_plan_info(const nsg_plan* plan, int32_t* chunk, int32_t* tasks_per_warp, int32_t minb[2],
+nsg_status nsg_plan_info(const nsg_plan* plan, int32_t chunk[2], int32_t tasks_per_warp[2], int32_t minb[2],
                          int32_t* timed) {
     API_BEGIN
     need(plan, "plan");
-    if (chunk) *chunk = plan->tiling.chunk;
-    if (tasks_per_warp) *tasks_per_warp = plan->tiling.tasks_per_warp;
+    for (int w = 0; w < 2; w++) {
+        if (chunk) chunk[w] = plan->tiling.chunk[w];
+        if (tasks_per_warp) tasks_per_warp[w] = plan->tiling.tasks_per_warp[w];
+    }
     if (minb) {
         minb[0] = plan->tiling.minb[0];
         minb[1] = plan->tiling.minb[1];
@@ -2403,6 +2498,55 @@ nsg_status nsg_debug_t_tensor(uint32_t t, nsg_state** out) {
     nsg_status rc = nsg_state_from_terms(t, chi, bG.data(), bF.data(), bM.data(), bgam.data(), bv.data(), bs.data(),
                                          ph.data(), ck.data(), cr.data(), nullptr, gf, out);
     if (rc != NSG_OK) return rc;
+    API_END
+}
+
+nsg_status nsg_toffoli_tensor_state(uint32_t num_tensors, nsg_state** out) {
+    API_BEGIN
+    need(out, "out");
+    *out = nullptr;
+    // construct_toffoli_tensor_state (magic_states/toffoli_state.rs:33-40).
+    if (num_tensors == 0)
+        raise(NSG_ERR_INVALID_NUM_QUBITS, 0, -1, "Number of qubits must be greater than zero, got 0.");
+    if (num_tensors > 21)
+        raise(NSG_ERR_TOO_WIDE, 3 * (int64_t)num_tensors, 63, "%u Toffoli states need %u qubits; at most 21 (63 qubits)",
+              num_tensors, 3 * num_tensors);
+    // construct_toffoli_state (toffoli_state.rs:12-31): |0+0⟩ and |1⟩⊗Bell, each with 2^{-1/2}.
+    HostCH a = HostCH::zero_state(3), b = HostCH::zero_state(3);
+    a.left_h(1);
+    b.left_x(0);
+    b.left_h(1);
+    b.left_cx(1, 2);
+    const HostCH* terms[2] = {&a, &b};
+    std::vector<uint8_t> bG(18), bF(18), bM(18), bgam(6), bv(6), bs(6), ph(2), ck(2, 0);
+    std::vector<int32_t> cr(2, 1);
+    for (int i = 0; i < 2; i++) {
+        const HostCH& c = *terms[i];
+        for (int r = 0; r < 3; r++) {
+            for (int q = 0; q < 3; q++) {
+                bG[i * 9 + r * 3 + q] = hbit(c.G[r].w, q);
+                bF[i * 9 + r * 3 + q] = hbit(c.F[r].w, q);
+                bM[i * 9 + r * 3 + q] = hbit(c.M[r].w, q);
+            }
+            bgam[i * 3 + r] = (uint8_t)(2 * c.gam[r]);  // the dump's γ is the Z8 exponent, 2·(power of i)
+            bv[i * 3 + r] = hbit(c.v, r);
+            bs[i * 3 + r] = hbit(c.s, r);
+        }
+        ph[i] = (uint8_t)c.phase;
+    }
+    const double gf[2] = {1.0, 0.0};
+    nsg_state* base = nullptr;
+    nsg_status rc = nsg_state_from_terms(3, 2, bG.data(), bF.data(), bM.data(), bgam.data(), bv.data(), bs.data(),
+                                         ph.data(), ck.data(), cr.data(), nullptr, gf, &base);
+    if (rc != NSG_OK) return rc;
+    std::unique_ptr<nsg_state> base_owner(base), acc;  // acc empty: the result is the base itself
+    for (uint32_t k = 1; k < num_tensors; k++) {  // construct(k) = construct(k-1).kron(construct(1))
+        nsg_state* next = nullptr;
+        rc = nsg_state_kron(acc ? acc.get() : base, base, &next);
+        if (rc != NSG_OK) return rc;
+        acc.reset(next);
+    }
+    *out = acc ? acc.release() : base_owner.release();
     API_END
 }
 

@@ -121,6 +121,14 @@ class QuantumState:
         return [QuantumState(C.c_void_p(hs[i])) for i in range(k)]
 
     @staticmethod
+    def toffoli_tensor(num_tensors: int) -> "QuantumState":
+        """|Toffoli⟩^{⊗k} on 3k qubits, 2^k terms (construct_toffoli_tensor_state,
+        crates/necstar/src/state/magic_states/toffoli_state.rs:12-40)."""
+        h = C.c_void_p()
+        check(_ffi.load().nsg_toffoli_tensor_state(num_tensors, C.byref(h)))
+        return QuantumState(h)
+
+    @staticmethod
     def debug_t_tensor(t: int) -> "QuantumState":
         """The device expansion of |T⟩^{⊗t} as a state (terms in the reference's order)."""
         h = C.c_void_p()
@@ -402,11 +410,17 @@ class BatchPlan:
 
     @property
     def tiling(self) -> dict:
-        chunk, tpw, timed = C.c_int32(), C.c_int32(), C.c_int32()
-        minb = (C.c_int32 * 2)()
-        check(_ffi.load().nsg_plan_info(self._h, C.byref(chunk), C.byref(tpw), minb, C.byref(timed)))
-        return {"chunk": chunk.value, "tasks_per_warp": tpw.value, "minb_rows32": minb[0], "minb_rows64": minb[1],
-                "timed": bool(timed.value)}
+        """Per row width (32- and 64-bit rows; 0 where the plan has none): kets per chunk,
+        tasks per resident warp, kernel variant; and whether creation timed candidates."""
+        chunk, tpw, minb = (C.c_int32 * 2)(), (C.c_int32 * 2)(), (C.c_int32 * 2)()
+        timed = C.c_int32()
+        check(_ffi.load().nsg_plan_info(self._h, chunk, tpw, minb, C.byref(timed)))
+        out = {"timed": bool(timed.value)}
+        for w, name in ((0, "rows32"), (1, "rows64")):
+            out[f"chunk_{name}"] = chunk[w]
+            out[f"tasks_per_warp_{name}"] = tpw[w]
+            out[f"minb_{name}"] = minb[w]
+        return out
 
 
 def exp_values_multi(states, paulis_per_state, precision: int = PRECISION_FP64) -> list[np.ndarray]:

@@ -417,3 +417,25 @@ def test_qasm_circuit_known_answer(gpu_pkg):
     st = gpu_pkg.QuantumState.from_circuit(c)
     assert close(st.exp_value(gpu_pkg.PauliString.from_str("ZII")), 0.5)
     assert close(st.norm(), 1.0)
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 5, 8])
+def test_toffoli_tensor_state_bit_exact(gpu_pkg, oracle, k):
+    """|Toffoli⟩^{⊗k} (magic_states/toffoli_state.rs:12-40): every term equal to the oracle's."""
+    st = gpu_pkg.QuantumState.toffoli_tensor(k)
+    ref = oracle.OracleState.toffoli_tensor(k)
+    assert (st.num_qubits, st.stabilizer_rank) == (3 * k, 2 ** k)
+    assert_same_terms(st.export_terms(), ref.export_terms())
+    if k <= 2:
+        assert np.abs(st.to_statevector() - ref.to_statevector()).max() < 1e-12
+    assert close(st.norm(), 1.0)
+
+
+def test_toffoli_tensor_state_limits(gpu_pkg):
+    from stab_decomp_simulator_rust_gb300 import NecstarError
+    with pytest.raises(NecstarError) as e:
+        gpu_pkg.QuantumState.toffoli_tensor(0)
+    assert e.value.code == 2
+    with pytest.raises(NecstarError) as e:
+        gpu_pkg.QuantumState.toffoli_tensor(22)
+    assert e.value.code == 105

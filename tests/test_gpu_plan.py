@@ -51,8 +51,9 @@ def test_plan_matches_direct_and_oracle(gpu_pkg, oracle, precision):
             _, ex = ref.exp_value(0, plists[c][o].ops)
             assert abs(got[c][o] - ex) <= TOL * max(1.0, abs(ex)), (c, o)
     t = plan.tiling
-    assert t["minb_rows32"] in (2, 3, 4, 5) and t["minb_rows64"] in (2, 3, 4, 5)
-    assert t["chunk"] > 0 and t["tasks_per_warp"] > 0
+    for w in ("rows32", "rows64"):  # SPECS has states of both row widths
+        assert t[f"minb_{w}"] in (2, 3, 4, 5)
+        assert t[f"chunk_{w}"] in (16, 32, 64) and t[f"tasks_per_warp_{w}"] in (4, 8, 16)
 
 
 def test_plan_sees_gates_applied_in_place(gpu_pkg):
@@ -96,8 +97,47 @@ def test_plan_tuning_cache(gpu_pkg):
     p1 = gpu_pkg.BatchPlan(states, plists)
     p2 = gpu_pkg.BatchPlan(states, plists)  # same device and workload class
     assert not p2.tiling["timed"]
-    assert p2.tiling["minb_rows64"] == p1.tiling["minb_rows64"]
+    assert p2.tiling == dict(p1.tiling, timed=False)
     assert close_arrays(p1.run()[0], p2.run()[0], 1e-12)
+
+
+_CACHE_CHILD = r"""
+import json, sys
+sys.path.insert(0, {root!r})
+import numpy as np
+import stab_decomp_simulator_rust_gb300 as pkg
+from stab_decomp_simulator_rust_gb300 import workloads as W
+g = W.random_clifford_t_circuit(36, 500, 12, 313)
+st = pkg.QuantumState.from_gates(36, g)
+ps = [pkg.PauliString.dense(p) for p in W.random_dense_paulis(36, 24, 314)]
+plan = pkg.BatchPlan([st], [ps])
+print(json.dumps(plan.tiling))
+"""
+
+
+def test_plan_tuning_cache_file_round_trip(gpu_pkg, tmp_path):
+    """NSG_TUNE_CACHE: a first process times the candidates and appends its
+    choice (variant, tasks per warp, chunk); a second process reads it back
+    and takes the same tiling without timing."""
+    import json
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cache = tmp_path / "tune.jsonl"
+    env = dict(os.environ, NSG_TUNE_CACHE=str(cache))
+    code = _CACHE_CHILD.format(root=root)
+    first = json.loads(subprocess.run([sys.executable, "-c", code], env=env, check=True, capture_output=True,
+                                      text=True).stdout.strip().splitlines()[-1])
+    lines = [json.loads(x) for x in cache.read_text().splitlines()]
+    assert first["timed"] and len(lines) == 1
+    assert {"key", "minb", "tasks_per_warp", "chunk"} <= set(lines[0])
+    assert (lines[0]["minb"], lines[0]["tasks_per_warp"], lines[0]["chunk"]) == \
+        (first["minb_rows64"], first["tasks_per_warp_rows64"], first["chunk_rows64"])
+    second = json.loads(subprocess.run([sys.executable, "-c", code], env=env, check=True, capture_output=True,
+                                       text=True).stdout.strip().splitlines()[-1])
+    assert not second["timed"]
+    assert second == dict(first, timed=False)
 
 
 def test_empty_plan(gpu_pkg):

@@ -257,3 +257,17 @@ def test_measure_uses_the_seeded_stream(oracle):
         st = oracle.OracleState.from_circuit(n, plus)
         u = oracle.random_doubles(seed, n)
         assert st.measure(list(range(n)), seed) == [bool(x >= 0.5) for x in u]
+
+
+def test_toffoli_state_statevector(oracle):
+    """construct_toffoli_state (magic_states/toffoli_state.rs:5-9): (|000⟩ + |100⟩ + |010⟩ + |111⟩)/2,
+    qubit 0 first in the text form, i.e. the little-endian indices 0, 1, 2, 7."""
+    sv = oracle.OracleState.toffoli_tensor(1).to_statevector()
+    want = np.zeros(8, complex)
+    want[[0, 1, 2, 7]] = 0.5
+    assert np.abs(sv - want).max() < 1e-12
+    two = oracle.OracleState.toffoli_tensor(2)
+    assert (two.num_qubits, two.stabilizer_rank) == (6, 4)
+    assert np.abs(two.to_statevector() - np.kron(want, want)).max() < 1e-12  # kron puts the new factor on top
+    with pytest.raises(ValueError):
+        oracle.OracleState.toffoli_tensor(0)
