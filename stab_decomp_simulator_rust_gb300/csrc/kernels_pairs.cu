@@ -425,6 +425,13 @@ __device__ __forceinline__ void transpose_lower(const uint64_t (&L)[2], uint64_t
     T[1] = (uint64_t)dd << 32;
 }
 
+// Bit `lane` of half k of a row mask (the lane's own row in slot k), tested on
+// the 32-bit half that holds it.
+template <typename Word>
+__device__ __forceinline__ bool own_bit(Word x, int k, uint32_t lbit) {
+    return ((uint32_t)(sizeof(Word) == 8 ? ((uint64_t)x >> (32 * k)) : (uint64_t)x) & lbit) != 0;
+}
+
 template <typename Word, int RPL>
 __device__ __forceinline__ Word row_of(const Word (&R)[RPL], int q) {  // row q, from its lane
     return shfl<Word>((RPL > 1 && q >= 32) ? R[RPL - 1] : R[0], q & 31);
@@ -440,9 +447,10 @@ __device__ __forceinline__ Word row_of(const Word (&R)[RPL], int q) {  // row q,
 // L_a ± 1 on T (the per-observable part of the carry is applied by the caller).
 template <typename Word, int RPL>
 __device__ __forceinline__ void g_expand(Word (&J)[RPL], Word& hs, Word& L0, Word T, const Word (&own)[RPL]) {
+    const uint32_t lbit = (uint32_t)own[0];
 #pragma unroll
     for (int k = 0; k < RPL; k++)
-        if (T & own[k]) J[k] ^= T & ~own[k];
+        if (own_bit<Word>(T, k, lbit)) J[k] ^= T ^ own[k];  // own bit set in T: flip every other bit of T
     hs ^= T & ~L0;
     L0 ^= T;
 }
@@ -455,18 +463,19 @@ __device__ __forceinline__ void g_subst(int kq, Word lp, const bool (&c)[NG], Wo
     const Word R = row_of<Word, RPL>(J, kq) & alive & ~kb;
 #pragma unroll
     for (int k = 0; k < RPL; k++) {  // z_k·(R·z) → (lp·z)(R·z): J ^= lp·Rᵀ + R·lpᵀ
+        const uint32_t lbit = (uint32_t)own[0];
         Word u = 0;
-        if (lp & own[k]) u ^= R;
-        if (R & own[k]) u ^= lp;
+        if (own_bit<Word>(lp, k, lbit)) u ^= R;
+        if (own_bit<Word>(R, k, lbit)) u ^= lp;
         J[k] ^= u;
     }
     hs ^= lp & R;  // its diagonal terms z_a² = z_a
-    const bool lowk = (L0 >> kq) & 1, hsk = (hs >> kq) & 1;
+    const bool lowk = (L0 & kb) != 0, hsk = (hs & kb) != 0;
     alive &= ~kb;
 #pragma unroll
     for (int g = 0; g < NG; g++) {
         if (c[g]) h[g] ^= R;
-        const bool hb = hsk ^ (bool)((h[g] >> kq) & 1);
+        const bool hb = hsk ^ ((h[g] & kb) != 0);
         if (!lowk) {  // (-1)^{hb·(c ⊕ lp·z)}
             if (hb && c[g]) ph[g] += 4;
             if (hb) h[g] ^= lp;
@@ -710,7 +719,7 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                     const int gm = (int)((gamV >> (2 * k)) & 3) + gsum + 2 * parity<Word>(yP[k] & FV[k]);
                     g0 |= (Word)__ballot_sync(FULL, gm & 1) << (32 * k);
                     g1 |= (Word)__ballot_sync(FULL, gm & 2) << (32 * k);
-                    diag |= (Word)__ballot_sync(FULL, (Kr[k] & own[k]) != 0) << (32 * k);
+                    diag |= (Word)__ballot_sync(FULL, own_bit<Word>(Kr[k], k, (uint32_t)own[0])) << (32 * k);
                     fvs |= (Word)__ballot_sync(FULL, parity<Word>(fD[k] & w)) << (32 * k);
                     Lw[k] = Kr[k] & (own[k] - 1);
                 }
@@ -761,15 +770,15 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                 // constraints (z·F)_b = rhs_b for b ∉ v_B, by substitution
                 Word crem = cons;
                 while (crem) {
-                    const int b = ffs0<Word>(crem);
-                    crem &= crem - 1;
+                    const Word bb = crem & (~crem + 1);  // the lowest remaining constraint column
+                    crem ^= bb;
                     Word l = 0;
 #pragma unroll
-                    for (int k = 0; k < RPL; k++) l |= (Word)__ballot_sync(FULL, (Fc[k] >> b) & 1) << (32 * k);
+                    for (int k = 0; k < RPL; k++) l |= (Word)__ballot_sync(FULL, (Fc[k] & bb) != 0) << (32 * k);
                     l &= alive;
                     bool c[NG];
 #pragma unroll
-                    for (int g = 0; g < NG; g++) c[g] = (rhs[g] >> b) & 1;
+                    for (int g = 0; g < NG; g++) c[g] = (rhs[g] & bb) != 0;
                     if (l == 0) {  // a consistency condition
 #pragma unroll
                         for (int g = 0; g < NG; g++) zero[g] |= c[g];
@@ -780,7 +789,7 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                     const Word Fk = row_of<Word, RPL>(Fc, kq);
 #pragma unroll
                     for (int k = 0; k < RPL; k++)
-                        if (lp & own[k]) Fc[k] ^= Fk;
+                        if (own_bit<Word>(lp, k, (uint32_t)own[0])) Fc[k] ^= Fk;
 #pragma unroll
                     for (int g = 0; g < NG; g++)
                         if (c[g]) rhs[g] ^= Fk;
@@ -808,25 +817,26 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         Word iso = 0;
 #pragma unroll
                         for (int k = 0; k < RPL; k++)
-                            iso |= (Word)__ballot_sync(FULL, (alive & own[k]) && !(J[k] & alive & ~own[k])) << (32 * k);
+                            iso |= (Word)__ballot_sync(FULL, own_bit<Word>(alive, k, (uint32_t)own[0]) &&
+                                                                 !(J[k] & alive & ~own[k])) << (32 * k);
                         IE |= iso & ~L0;
                         IO |= iso & L0;
                         alive &= ~iso;
                         continue;
                     }
                     alive &= ~jb;
-                    if ((L0 >> jq) & 1) {  // 1 + i^{L_j}(-1)^{S·z} = √2·ω^{±1}·i^{∓S·z}
+                    if (L0 & jb) {  // 1 + i^{L_j}(-1)^{S·z} = √2·ω^{±1}·i^{∓S·z}
                         IO |= jb;
 #pragma unroll
                         for (int g = 0; g < NG; g++)
-                            if (((hs ^ h[g]) >> jq) & 1) h[g] ^= S;
+                            if ((hs ^ h[g]) & jb) h[g] ^= S;
                         g_expand<Word, RPL>(J, hs, L0, S, own);
                     } else {  // 1 + (-1)^{hb + S·z} = 2·δ(S·z = hb), S ≠ 0 here
                         r -= 2;
                         bool hb[NG];
-                        const bool hsj = (hs >> jq) & 1;
+                        const bool hsj = (hs & jb) != 0;
 #pragma unroll
-                        for (int g = 0; g < NG; g++) hb[g] = hsj ^ (bool)((h[g] >> jq) & 1);
+                        for (int g = 0; g < NG; g++) hb[g] = hsj ^ ((h[g] & jb) != 0);
                         g_subst<Word, RPL, NG>(ffs0<Word>(S), S & (S - 1), hb, J, hs, L0, alive, h, ph, own);
                     }
                 }
