@@ -115,8 +115,15 @@ struct DBuf {
         }
     }
     void rehome(cudaStream_t s) { st = s; }
+    // Freed with cudaFree (it waits for the device), not stream-ordered: after
+    // states made of hundreds of per-stream buffers were freed with
+    // cudaFreeAsync, later stream-ordered allocations and launches slowed down
+    // 10-30x on GB300 (a second batch of 512 compiles: 11-33 s instead of
+    // 1.2 s); with cudaFree every repeat took 1.2 s.  cudaFree waits for the
+    // work on the device, so a launch still reading the buffer is never cut
+    // short; no buffer is freed inside a stream capture.
     void release() {
-        if (p) cudaFreeAsync(p, st);
+        if (p) cudaFree(p);
         p = nullptr;
         n = 0;
     }
@@ -871,20 +878,22 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
                 d.scale_re = u->a->gf_re * u->a->gf_re + u->a->gf_im * u->a->gf_im;
                 d.scale_im = 0.0;
             }
+            // Ket-major chunks: ket block kb (kets kb·chunk ..) against every bra that
+            // pairs with it (triangular: the bras up to the block's last ket).
             int64_t nch;
+            d.nblk = (chiB + chunk - 1) / chunk;
             if (u->triangular) {
                 off_at[q] = offs.size();
                 int64_t acc = 0;
-                for (int64_t i = 0; i < chiA; i++) {
+                for (int64_t kb = 0; kb < d.nblk; kb++) {
                     offs.push_back(acc);
-                    acc += (chiA - i + chunk - 1) / chunk;
+                    acc += std::min<int64_t>((kb + 1) * chunk, chiA);
                 }
                 offs.push_back(acc);
                 nch = acc;
                 b.pairs += (uint64_t)(chiA * (chiA + 1) / 2);
             } else {
-                d.cpr = (chiB + chunk - 1) / chunk;
-                nch = chiA * d.cpr;
+                nch = chiA * d.nblk;
                 b.pairs += (uint64_t)(chiA * chiB);
             }
             d.nchunks = nch;
@@ -918,12 +927,20 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
             auto pairs_before = [&](size_t q, int64_t c) -> int64_t {
                 const PairUnit* u = b.live[sel[q]];
                 const int64_t chiA = u->a->t.chi, chiB = u->b->t.chi;
-                if (!u->triangular)
-                    return (c / descs[q].cpr) * chiB + std::min<int64_t>((c % descs[q].cpr) * chunk, chiB);
+                if (!u->triangular) {  // full blocks of χ_A bras, then r bras of block kb
+                    const int64_t kb = c / chiA, r = c - kb * chiA;
+                    const int64_t a = std::min<int64_t>(kb * chunk, chiB), e = std::min<int64_t>(a + chunk, chiB);
+                    return a * chiA + r * (e - a);
+                }
+                const int64_t nblk = descs[q].nblk;
                 const int64_t* off = offs.data() + off_at[q];
-                const int64_t i = (int64_t)(std::upper_bound(off, off + chiA + 1, c) - off) - 1;
-                if (i >= chiA) return chiA * (chiA + 1) / 2;
-                return i * chiA - i * (i - 1) / 2 + std::min<int64_t>((c - off[i]) * chunk, chiA - i);
+                const int64_t kb = (int64_t)(std::upper_bound(off, off + nblk + 1, c) - off) - 1;
+                if (kb >= nblk) return chiA * (chiA + 1) / 2;
+                // every pair with j below the block, then bras 0 .. r-1 against it
+                const int64_t a = kb * chunk, e = std::min<int64_t>(a + chunk, chiA), r = c - off[kb];
+                int64_t before = a * (a + 1) / 2;
+                if (r <= a) return before + r * (e - a);
+                return before + a * (e - a) + (r - a) * e - (r - a) * (a + r - 1) / 2;
             };
             ln.pairs_total = 0;
             for (size_t q = 0; q < sel.size(); q++) ln.pairs_total += pairs_before(q, descs[q].nchunks);
@@ -949,7 +966,7 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
         int64_t* d_ob = (int64_t*)(ln.blob.p + b_desc + b_db);
         int64_t* d_off = (int64_t*)(ln.blob.p + b_desc + b_db + b_ob);
         for (size_t q = 0; q < sel.size(); q++)
-            if (descs[q].triangular) descs[q].row_chunk_off = d_off + off_at[q];
+            if (descs[q].triangular) descs[q].blk_chunk_off = d_off + off_at[q];
         std::vector<unsigned char> hb(b_desc + b_db + b_ob + b_off);
         std::memcpy(hb.data(), descs.data(), b_desc);
         std::memcpy(hb.data() + b_desc, tbegin.data(), b_db);

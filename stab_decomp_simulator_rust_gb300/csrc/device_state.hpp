@@ -188,8 +188,8 @@ struct PairDesc {
     const uint8_t* pk = nullptr;   // [chiA][nobs] Z8 phase
     int triangular = 1;            // exp_value/norm (A == B, i ≤ j) vs inner product (all pairs)
     int complex_out = 0;
-    const int64_t* row_chunk_off = nullptr;  // triangular: [chiA+1] chunk prefix within the unit
-    int64_t cpr = 0;                         // rectangular: chunks per row
+    const int64_t* blk_chunk_off = nullptr;  // triangular: [nblk+1] chunk prefix of the ket blocks
+    int64_t nblk = 0;                        // ket blocks of `chunk` kets
     int64_t nchunks = 0;                     // chunks of the unit
     int64_t rec0 = 0;                        // first double of the unit's task records
     double scale_re = 1.0, scale_im = 0.0;   // |g|² or conj(g_a)·g_b

@@ -589,21 +589,26 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
         const int64_t c0 = tl * p.task_chunks, c1 = min(c0 + (int64_t)p.task_chunks, d->nchunks);
         double* rec = p.records + d->rec0 + tl * (int64_t)nobs * 8;  // this task's record
         for (int64_t lc = c0; lc < c1 && !timed_out; lc++) {
+            // Ket-major order: chunk lc is bra i against the ket block kb (kets
+            // kb·chunk .. +chunk), all bras of one block consecutive, so the warps
+            // working at one time share a few blocks of ket tables in L2.
             int64_t i, j0, j1;
-            if (tri) {
-                int64_t lo = 0, hi = d->A.chi;
+            if (tri) {  // block kb pairs with bras 0 .. min(kb·chunk + chunk, χ) - 1 (i ≤ j)
+                int64_t lo = 0, hi = d->nblk;
                 while (hi - lo > 1) {
                     int64_t mid = (lo + hi) >> 1;
-                    if (d->row_chunk_off[mid] <= lc) lo = mid;
+                    if (d->blk_chunk_off[mid] <= lc) lo = mid;
                     else hi = mid;
                 }
-                i = lo;
-                j0 = i + (lc - d->row_chunk_off[i]) * p.chunk;
-            } else {
-                i = lc / d->cpr;
-                j0 = (lc % d->cpr) * p.chunk;
+                i = lc - d->blk_chunk_off[lo];
+                j0 = max(i, lo * (int64_t)p.chunk);
+                j1 = min((lo + 1) * (int64_t)p.chunk, chiB);
+            } else {  // every block pairs with all χ_A bras
+                const int64_t kb = lc / d->A.chi;
+                i = lc - kb * d->A.chi;
+                j0 = kb * (int64_t)p.chunk;
+                j1 = min(j0 + (int64_t)p.chunk, chiB);
             }
-            j1 = min(j0 + (int64_t)p.chunk, chiB);
             if (i != cur_i) {  // a new bra: its frame rows, scalars, Pauli frames and G table
                 cur_i = i;
                 const FrameView& fr = d->fr;
