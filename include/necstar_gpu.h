@@ -227,7 +227,7 @@ nsg_status nsg_exp_value_counts(const nsg_state* state, const nsg_pauli* paulis,
 /* Tiling of the direct (uncaptured) pair sums of this process: kets per
  * chunk and tasks per resident warp of the persistent pair launch; 0 takes
  * the tuned choice of the workload class if a plan tuned one, else the
- * default (32 and 8).  Results do not depend on it beyond FP rounding of the
+ * default (32 and 64).  Results do not depend on it beyond FP rounding of the
  * partial sums (no reference counterpart). */
 nsg_status nsg_set_pair_tiling(int32_t chunk, int32_t tasks_per_warp);
 
@@ -257,8 +257,8 @@ nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pauli* pauli,
  * operation that changes a state's rank, width or global factor (projection,
  * discard, measurement) or frees it makes nsg_plan_run fail with
  * NSG_ERR_INVALID_ARGUMENT.  Creation picks, for each row width, the
- * pair-kernel variant (2-5 blocks per SM), the tasks per resident warp (4, 8,
- * 16) and the kets per chunk (16, 32, 64), in that order, by timing the
+ * pair-kernel variant (2-5 blocks per SM), the tasks per resident warp (16,
+ * 64, 256) and the kets per chunk (16, 32, 64), in that order, by timing the
  * candidates on the plan's own work (whole launches when short, else the
  * first two tasks per resident warp); the choice is remembered per device
  * and workload class for the process (direct calls of the same class use it
