@@ -20,18 +20,21 @@ constexpr int WARPS = 4;
 constexpr int OPS_CHUNK = 2048;
 constexpr int kCompileWarps = 4;  // warps per block of the compile kernel
 
-template <int W>
-using Eng = WarpCH<uint64_t, W, 2 * W>;
+// A warp-held term with W 64-bit words per row in RPL row slots of 32 rows
+// (RPL = 2W holds every row of the storage; the compile kernel uses RPL = 3
+// for widths 65-96).
+template <int W, int RPL = 2 * W>
+using Eng = WarpCH<uint64_t, W, RPL>;
 
 // ---- load / store a term between HBM (any storage W) and a warp engine -----
-template <int W>
-__device__ __forceinline__ void load_term(Eng<W>& e, const TermsView& tv, int64_t term) {
+template <int W, int RPL = 2 * W>
+__device__ __forceinline__ void load_term(Eng<W, RPL>& e, const TermsView& tv, int64_t term) {
     e.n = tv.n;
     e.err = 0;
     e.phase = tv.phase[term];
     e.gam = 0;
 #pragma unroll
-    for (int k = 0; k < 2 * W; k++) {
+    for (int k = 0; k < RPL; k++) {
         int r = 32 * k + e.lane;
 #pragma unroll
         for (int w = 0; w < W; w++) {
@@ -59,19 +62,21 @@ __device__ __forceinline__ void load_term(Eng<W>& e, const TermsView& tv, int64_
     }
 }
 
-template <int W>
-__device__ __forceinline__ void store_term(const Eng<W>& e, const TermsView& tv, int64_t term) {
+template <int W, int RPL = 2 * W>
+__device__ __forceinline__ void store_term(const Eng<W, RPL>& e, const TermsView& tv, int64_t term) {
 #pragma unroll
-    for (int k = 0; k < 2 * W; k++) {
+    for (int k = 0; k < 4; k++) {  // every row slot of the storage; slots the engine does not hold are zero
         int r = 32 * k + e.lane;
         if (r < tv.R) {
 #pragma unroll
             for (int w = 0; w < 2; w++) {
                 if (w < tv.W) {
+                    const bool held = k < RPL && w < W;
+                    const int kk = k < RPL ? k : 0, ww = w < W ? w : 0;
                     size_t idx = ((size_t)term * tv.R + r) * tv.W + w;
-                    tv.G[idx] = (w < W) ? e.G[k].w[(w < W) ? w : 0] : 0;
-                    tv.F[idx] = (w < W) ? e.F[k].w[(w < W) ? w : 0] : 0;
-                    tv.M[idx] = (w < W) ? e.M[k].w[(w < W) ? w : 0] : 0;
+                    tv.G[idx] = held ? e.G[kk].w[ww] : 0;
+                    tv.F[idx] = held ? e.F[kk].w[ww] : 0;
+                    tv.M[idx] = held ? e.M[kk].w[ww] : 0;
                 }
             }
         }
@@ -79,7 +84,7 @@ __device__ __forceinline__ void store_term(const Eng<W>& e, const TermsView& tv,
     // γ planes by ballot: slot k covers rows 32k..32k+31 = word k/2, half k%2.
     uint64_t gl[2] = {0, 0}, gh[2] = {0, 0};
 #pragma unroll
-    for (int k = 0; k < 2 * W; k++) {
+    for (int k = 0; k < RPL; k++) {
         int g = e.gam_of(k);
         uint32_t b0 = __ballot_sync(dev::FULL, g & 1);
         uint32_t b1 = __ballot_sync(dev::FULL, (g >> 1) & 1);
@@ -100,8 +105,8 @@ __device__ __forceinline__ void store_term(const Eng<W>& e, const TermsView& tv,
     }
 }
 
-template <int W>
-__device__ __forceinline__ void apply_prim(Eng<W>& e, uint32_t code) {
+template <int W, int RPL = 2 * W>
+__device__ __forceinline__ void apply_prim(Eng<W, RPL>& e, uint32_t code) {
     uint32_t op = code & 0xff, a = (code >> 8) & 0xff, b = (code >> 16) & 0xff;
     switch (op) {
         case P_H: e.left_h(a); break;
@@ -119,7 +124,7 @@ __device__ __forceinline__ void apply_prim(Eng<W>& e, uint32_t code) {
 // ---- compile ------------------------------------------------------------------
 // CW warps per block: a compile launch has one warp per T-term, often only a few
 // per SM, so small blocks spread them evenly over the SMs.
-template <int W, int CW>
+template <int W, int RPL, int CW>
 __global__ void __launch_bounds__(CW * 32) compile_kernel(
     const uint32_t* __restrict__ ops, int nops, int n, int t, int64_t chi_t,
     const uint64_t* __restrict__ tG, const uint64_t* __restrict__ tF, const uint64_t* __restrict__ tM,
@@ -132,13 +137,13 @@ __global__ void __launch_bounds__(CW * 32) compile_kernel(
     const bool active = term < chi_t;
     const int width = n + t;
 
-    Eng<W> e;
+    Eng<W, RPL> e;
     e.lane = lane;
     e.init_zero(width);
     if (active) {
         // kron(|0^n⟩, T-term) (form/kron.rs:12-59): T rows shifted by n rows and n columns.
 #pragma unroll
-        for (int k = 0; k < 2 * W; k++) {
+        for (int k = 0; k < RPL; k++) {
             int r = 32 * k + lane;
             if (r >= n && r < width) {
                 int tr = r - n;
@@ -180,7 +185,7 @@ __global__ void __launch_bounds__(CW * 32) compile_kernel(
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) sops[i] = ops[base + i];
         __syncthreads();
         if (active && !e.err) {
-            for (int i = 0; i < cnt; i++) apply_prim<W>(e, sops[i]);
+            for (int i = 0; i < cnt; i++) apply_prim<W, RPL>(e, sops[i]);
         }
     }
     if (!active) return;
@@ -208,7 +213,7 @@ __global__ void __launch_bounds__(CW * 32) compile_kernel(
         out.coef_k[term] = tCk[term];
         out.coef_r[term] = tCr[term] - ndet;  // coeff.amplify(ndet) (scalar.rs:108-119)
     }
-    if (ok) store_term<W>(e, out, term);
+    if (ok) store_term<W, RPL>(e, out, term);
 }
 
 // ---- |T⟩^{⊗t} expansion --------------------------------------------------------
@@ -558,11 +563,14 @@ cudaError_t launch_compile(const uint32_t* d_ops, int nops, int n, int t, int64_
     constexpr int CW = kCompileWarps;
     dim3 grid((unsigned)((chi_t + CW - 1) / CW)), block(CW * 32);
     if (width <= 64)
-        compile_kernel<1, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
-                                                      tCk, tCr, out, keep, status);
+        compile_kernel<1, 2, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
+                                                         tCk, tCr, out, keep, status);
+    else if (width <= 96)  // three row slots: a quarter less work than the full 128 rows
+        compile_kernel<2, 3, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
+                                                         tCk, tCr, out, keep, status);
     else
-        compile_kernel<2, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
-                                                      tCk, tCr, out, keep, status);
+        compile_kernel<2, 4, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
+                                                         tCk, tCr, out, keep, status);
     return cudaGetLastError();
 }
 
