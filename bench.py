@@ -62,10 +62,12 @@ METRIC = "Pauli ⟨P⟩/s and CH inner products/s, mixed+batched vs plain FP64 @
 UNIT = "<P>/s"
 WORKLOAD = "512 circuits, n~U[8,64], t~U[4,32], 20n {H,S,CX}, 16 dense Paulis each (seed 4)"
 
-# DRAM bytes (read + write) per launch of the 64-bit-row pair kernel on the
-# default workload, from one ncu capture of the current build
-# (dram__bytes_read.sum + dram__bytes_write.sum; profiles/pair_kernel_batch512.md).
-PAIR_TRAFFIC_BYTES = None
+# DRAM bytes (read + write) of the 64-bit-row pair launch of one step of the
+# default workload, with the tiling its plan tunes (16 kets per chunk, 256
+# tasks per resident warp), from one ncu capture of this build:
+# dram__bytes_read.sum 3.31 GB + dram__bytes_write.sum 0.48 GB (the ket
+# tables ≈ 2 GB read about once, task records, frames).
+PAIR_TRAFFIC_BYTES = 3_310_000_000 + 483_440_000
 
 
 def dist_env():
@@ -449,7 +451,8 @@ def run_ours(args):
     achieved = ops / (pk_ms * 1e-3)
     roofline = {"bound": "int", "achieved": achieved / 1e12, "peak": word_peak / 1e12, "unit": "Tword-ops/s",
                 "frac": achieved / word_peak, "traffic": PAIR_TRAFFIC_BYTES,
-                "traffic_unit": "DRAM bytes per 64-bit-row launch (ncu)",
+                "traffic_unit": "DRAM bytes of the 64-bit-row launch of one step (ncu, tuned tiling); "
+                                "the ket tables it reads are ~2.0 GB",
                 "kernel": "pair_kernel (32- and 64-bit-row launches of one step)",
                 "peak_source": "measured on this GPU: LOP3 chains on every SM (nsg_probe_int_ops), "
                                "a 64-bit word = 2 int32 logic ops",
