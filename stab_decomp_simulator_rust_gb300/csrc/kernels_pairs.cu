@@ -513,10 +513,14 @@ __device__ __forceinline__ void exact_add(unsigned long long* bins, int& bin, in
 template <typename Word, int RPL, int NG, int MINB, bool EXACT>
 __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) {
     constexpr int GMAX = (8 * sizeof(Word)) / 4;  // groups of four rows (8 or 16)
-    // Unrolling of the table-lookup loops: full for 32-bit rows; for 64-bit
-    // rows partial, less with more observables per lane (code size and
-    // registers; from launch timings at n = 40 and 60).
-    constexpr int UNROLL_COMP = sizeof(Word) == 4 ? GMAX : (NG <= 2 ? 4 : 2);
+    // Unrolling of the table-lookup loops: full for 32-bit rows and for one
+    // observable group; for 64-bit rows with more groups partial, less with
+    // more observables per lane (code size and registers; from launch timings
+    // at n = 40 and 60 and on the 512-circuit workload).  The lookups go two
+    // groups at a time, so each accumulator takes one three-input XOR per
+    // 32-bit half for two table entries (the second masked off past the last
+    // group).
+    constexpr int UNROLL_COMP = sizeof(Word) == 4 ? GMAX : (NG == 1 ? GMAX : (NG <= 2 ? 4 : 2));
     constexpr int UNROLL_BRA = sizeof(Word) == 4 ? GMAX : (NG <= 2 ? GMAX : 2);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -693,26 +697,35 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                     fD[k] = yP[k] = Kr[k] = 0;
                     Y[k] = MV[k];
                 }
-#pragma unroll (UNROLL_COMP)
-                for (int g = 0; g < GMAX; g++) {
+#pragma unroll (UNROLL_COMP / 2 > 0 ? UNROLL_COMP / 2 : 1)
+                for (int g = 0; g < GMAX; g += 2) {
                     if (g < ngrp) {
+                        const bool two = g + 1 < ngrp;
                         const Word* TF = T + g * 16;
                         const Word* TP = T + (ngrp + g) * 16;
                         const Word* TK = T + (2 * ngrp + g) * 16;
 #pragma unroll
                         for (int k = 0; k < RPL; k++) {
-                            const int jf = nib<Word, RPL>(FV[k], g);
-                            fD[k] ^= TF[jf];
-                            yP[k] ^= TP[jf];
-                            Y[k] ^= TK[jf];
+                            const int j0 = nib<Word, RPL>(FV[k], g);
+                            const int j1 = two ? nib<Word, RPL>(FV[k], g + 1) + 16 : j0;
+                            const Word m = two ? ~(Word)0 : (Word)0;
+                            fD[k] ^= TF[j0] ^ (TF[j1] & m);
+                            yP[k] ^= TP[j0] ^ (TP[j1] & m);
+                            Y[k] ^= TK[j0] ^ (TK[j1] & m);
                         }
                     }
                 }
-#pragma unroll (UNROLL_BRA)
-                for (int g = 0; g < GMAX; g++) {
+#pragma unroll (UNROLL_BRA / 2 > 0 ? UNROLL_BRA / 2 : 1)
+                for (int g = 0; g < GMAX; g += 2) {
                     if (g < ngrp) {
+                        const bool two = g + 1 < ngrp;
+                        const Word m = two ? ~(Word)0 : (Word)0;
 #pragma unroll
-                        for (int k = 0; k < RPL; k++) Kr[k] ^= tbA[g * 16 + nib<Word, RPL>(Y[k], g)];
+                        for (int k = 0; k < RPL; k++) {
+                            const int j0 = g * 16 + nib<Word, RPL>(Y[k], g);
+                            const int j1 = two ? (g + 1) * 16 + nib<Word, RPL>(Y[k], g + 1) : j0;
+                            Kr[k] ^= tbA[j0] ^ (tbA[j1] & m);
+                        }
                     }
                 }
                 // γ_D (eq. of the composed tableau) and the uniform bit planes
