@@ -487,6 +487,65 @@ __device__ __forceinline__ void g_subst(int kq, Word lp, const bool (&c)[NG], Wo
     if (lowk) g_expand<Word, RPL>(J, hs, L0, lp, own);
 }
 
+template <typename Word>
+__device__ __forceinline__ int fls0(Word x);  // index of the highest set bit
+template <>
+__device__ __forceinline__ int fls0<uint32_t>(uint32_t x) { return 31 - __clz(x); }
+template <>
+__device__ __forceinline__ int fls0<uint64_t>(uint64_t x) { return 63 - __clzll((long long)x); }
+
+// Sums out alive variables while one is left in `until` (the summation rounds
+// of the pair kernel).  A variable removed from `alive` keeps its bits of hs,
+// h and L0 from then on (every later update is masked by alive), so the
+// factors that depend only on its own bits are taken at the end: IE collects
+// summed-out variables with even L (a factor 2·δ(hb = 0)), IO those with odd L
+// (a factor √2·ω^{1-2hb}).  HIGH: pivots (and substituted variables) are the
+// highest candidates instead of the lowest.
+template <typename Word, int RPL, int NG, bool HIGH>
+__device__ __forceinline__ void sum_out(Word (&J)[RPL], Word& hs, Word& L0, Word& alive, Word& IE, Word& IO, int& r,
+                                        Word (&h)[NG], int (&ph)[NG], const Word (&own)[RPL], const Word until) {
+    while (alive & until) {
+        // the next variable, with even L if there is one (an even step removes
+        // two variables, which leaves fewer steps in all)
+        const Word cand = alive & until;
+        const Word even = cand & ~L0;
+        const int jq = HIGH ? fls0<Word>(even ? even : cand) : ffs0<Word>(even ? even : cand);
+        const Word jb = (Word)1 << jq;
+        const Word S = row_of<Word, RPL>(J, jq) & alive & ~jb;
+        if (!S) {
+            // it is isolated (coupled to no other alive variable): all isolated
+            // variables factor out together, found by one ballot.  An elimination
+            // never touches an isolated variable (its row and column are zero
+            // among the alive ones), so they can wait until a pivot is one of them.
+            Word iso = 0;
+#pragma unroll
+            for (int k = 0; k < RPL; k++)
+                iso |= (Word)__ballot_sync(FULL, own_bit<Word>(alive, k, (uint32_t)own[0]) &&
+                                                     !(J[k] & alive & ~own[k])) << (32 * k);
+            IE |= iso & ~L0;
+            IO |= iso & L0;
+            alive &= ~iso;
+            continue;
+        }
+        alive &= ~jb;
+        if (L0 & jb) {  // 1 + i^{L_j}(-1)^{S·z} = √2·ω^{±1}·i^{∓S·z}
+            IO |= jb;
+#pragma unroll
+            for (int g = 0; g < NG; g++)
+                if ((hs ^ h[g]) & jb) h[g] ^= S;
+            g_expand<Word, RPL>(J, hs, L0, S, own);
+        } else {  // 1 + (-1)^{hb + S·z} = 2·δ(S·z = hb), S ≠ 0 here
+            r -= 2;
+            bool hb[NG];
+            const bool hsj = (hs & jb) != 0;
+#pragma unroll
+            for (int g = 0; g < NG; g++) hb[g] = hsj ^ ((h[g] & jb) != 0);
+            const int kq = HIGH ? fls0<Word>(S) : ffs0<Word>(S);
+            g_subst<Word, RPL, NG>(kq, S ^ ((Word)1 << kq), hb, J, hs, L0, alive, h, ph, own);
+        }
+    }
+}
+
 // MINB: blocks per SM the register allocation must allow (the register cap is
 // 65536 / (128·MINB)); the launch picks it per workload (fewer blocks leave
 // more registers for many observables per lane).
@@ -813,50 +872,29 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         if (c[g]) rhs[g] ^= Fk;
                     g_subst<Word, RPL, NG>(kq, lp, c, J, hs, L0, alive, h, ph, own);
                 }
-                // summation.  A variable removed from `alive` keeps its bits of hs,
-                // h and L0 from then on (every later update is masked by alive),
-                // so the factors that depend only on its own bits are taken at the
-                // end: IE collects summed-out variables with even L (a factor
-                // 2·δ(hb = 0)), IO those with odd L (a factor √2·ω^{1-2hb}).
+                // summation (sum_out)
                 Word IE = 0, IO = 0;
-                while (alive) {
-                    // the next variable, with even L if there is one (an even step
-                    // removes two variables, which leaves fewer steps in all)
-                    const Word even = alive & ~L0;
-                    const int jq = ffs0<Word>(even ? even : alive);
-                    const Word jb = (Word)1 << jq;
-                    const Word S = row_of<Word, RPL>(J, jq) & alive & ~jb;
-                    if (!S) {
-                        // it is isolated (coupled to no other alive variable): all
-                        // isolated variables factor out together, found by one ballot.
-                        // An elimination never touches an isolated variable (its row
-                        // and column are zero among the alive ones), so they can wait
-                        // until a pivot is one of them.
-                        Word iso = 0;
+                if constexpr (sizeof(Word) == 8) {
+                    // The variables of rows 32..63 first (highest first), then the
+                    // rest on 32-bit words in one row slot: every update is masked by
+                    // `alive`, so once no variable is left in the high half nothing
+                    // above bit 31 changes again.
+                    sum_out<Word, RPL, NG, true>(J, hs, L0, alive, IE, IO, r, h, ph, own, ~(Word)0xffffffffu);
+                    uint32_t J32[1] = {(uint32_t)J[0]};
+                    const uint32_t own32[1] = {(uint32_t)own[0]};
+                    uint32_t hs32 = (uint32_t)hs, L032 = (uint32_t)L0, alive32 = (uint32_t)alive, IE32 = 0, IO32 = 0;
+                    uint32_t h32[NG];
 #pragma unroll
-                        for (int k = 0; k < RPL; k++)
-                            iso |= (Word)__ballot_sync(FULL, own_bit<Word>(alive, k, (uint32_t)own[0]) &&
-                                                                 !(J[k] & alive & ~own[k])) << (32 * k);
-                        IE |= iso & ~L0;
-                        IO |= iso & L0;
-                        alive &= ~iso;
-                        continue;
-                    }
-                    alive &= ~jb;
-                    if (L0 & jb) {  // 1 + i^{L_j}(-1)^{S·z} = √2·ω^{±1}·i^{∓S·z}
-                        IO |= jb;
+                    for (int g = 0; g < NG; g++) h32[g] = (uint32_t)h[g];
+                    sum_out<uint32_t, 1, NG, false>(J32, hs32, L032, alive32, IE32, IO32, r, h32, ph, own32, ~0u);
+                    const Word hi = ~(Word)0xffffffffu;
+                    hs = (hs & hi) | hs32;
 #pragma unroll
-                        for (int g = 0; g < NG; g++)
-                            if ((hs ^ h[g]) & jb) h[g] ^= S;
-                        g_expand<Word, RPL>(J, hs, L0, S, own);
-                    } else {  // 1 + (-1)^{hb + S·z} = 2·δ(S·z = hb), S ≠ 0 here
-                        r -= 2;
-                        bool hb[NG];
-                        const bool hsj = (hs & jb) != 0;
-#pragma unroll
-                        for (int g = 0; g < NG; g++) hb[g] = hsj ^ ((h[g] & jb) != 0);
-                        g_subst<Word, RPL, NG>(ffs0<Word>(S), S & (S - 1), hb, J, hs, L0, alive, h, ph, own);
-                    }
+                    for (int g = 0; g < NG; g++) h[g] = (h[g] & hi) | h32[g];
+                    IE |= IE32;
+                    IO |= IO32;
+                } else {
+                    sum_out<Word, RPL, NG, false>(J, hs, L0, alive, IE, IO, r, h, ph, own, ~(Word)0);
                 }
                 r -= 2 * popc<Word>(IE) + popc<Word>(IO);
 #pragma unroll
