@@ -273,7 +273,9 @@ struct ChunkAcc {
 // then a 48-byte trailer with the term's scalars (KetTrailer), and last the
 // table of G, which the pair kernel reads when the term is the bra.  Layout
 // per term: [F|P|K][ngrp][16] Words, trailer, [G][ngrp][16] Words; one bulk
-// copy of the first part brings everything the kernel reads of a ket.
+// copy of the first part brings everything the kernel reads of a ket.  ngrp
+// is ⌈n/4⌉ rounded up to an even count: the padding group is all zeros, so
+// the pair kernel looks groups up two at a time with no mask.
 struct KetTrailer {
     uint64_t gl, gh, v, s;  // γ planes, v, s (low word)
     uint8_t phase, coef_k, pad0, pad1;
@@ -331,7 +333,7 @@ __global__ void __launch_bounds__(FWARPS * 32) ket_tables_kernel(TermsView tv, i
             const int row = 4 * g + b;
             if (((idx >> b) & 1) && row < n) acc ^= sR[wid][mat][row];
         }
-        if (mat < 3) dst[e] = acc;
+        if (mat < 3) dst[(g * 16 + idx) * 3 + mat] = acc;
         else gdst[e - 3 * per] = acc;
     }
     if (lane == 0) {
@@ -509,9 +511,19 @@ __device__ __forceinline__ void sum_out(Word (&J)[RPL], Word& hs, Word& L0, Word
         // two variables, which leaves fewer steps in all)
         const Word cand = alive & until;
         const Word even = cand & ~L0;
-        const int jq = HIGH ? fls0<Word>(even ? even : cand) : ffs0<Word>(even ? even : cand);
-        const Word jb = (Word)1 << jq;
-        const Word S = row_of<Word, RPL>(J, jq) & alive & ~jb;
+        int jq;
+        Word jb, S;
+        if constexpr (HIGH && sizeof(Word) == 8) {  // candidates are in rows 32..63 only
+            const uint32_t e32 = (uint32_t)((uint64_t)even >> 32), c32 = (uint32_t)((uint64_t)cand >> 32);
+            const int q = 31 - __clz(e32 ? e32 : c32);
+            jq = 32 + q;
+            jb = (Word)(1u << q) << 32;
+            S = shfl<Word>(J[RPL - 1], q) & alive & ~jb;
+        } else {
+            jq = HIGH ? fls0<Word>(even ? even : cand) : ffs0<Word>(even ? even : cand);
+            jb = (Word)1 << jq;
+            S = row_of<Word, RPL>(J, jq) & alive & ~jb;
+        }
         if (!S) {
             // it is isolated (coupled to no other alive variable): all isolated
             // variables factor out together, found by one ballot.  An elimination
@@ -576,9 +588,8 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
     // observable group; for 64-bit rows with more groups partial, less with
     // more observables per lane (code size and registers; from launch timings
     // at n = 40 and 60 and on the 512-circuit workload).  The lookups go two
-    // groups at a time, so each accumulator takes one three-input XOR per
-    // 32-bit half for two table entries (the second masked off past the last
-    // group).
+    // groups at a time (ngrp is even), so each accumulator takes one
+    // three-input XOR per 32-bit half for two table entries.
     constexpr int UNROLL_COMP = sizeof(Word) == 4 ? GMAX : (NG == 1 ? GMAX : (NG <= 2 ? 4 : 2));
     constexpr int UNROLL_BRA = sizeof(Word) == 4 ? GMAX : (NG <= 2 ? GMAX : 2);
     extern __shared__ __align__(128) unsigned char smem_raw[];
@@ -759,31 +770,24 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
 #pragma unroll (UNROLL_COMP / 2 > 0 ? UNROLL_COMP / 2 : 1)
                 for (int g = 0; g < GMAX; g += 2) {
                     if (g < ngrp) {
-                        const bool two = g + 1 < ngrp;
-                        const Word* TF = T + g * 16;
-                        const Word* TP = T + (ngrp + g) * 16;
-                        const Word* TK = T + (2 * ngrp + g) * 16;
 #pragma unroll
                         for (int k = 0; k < RPL; k++) {
-                            const int j0 = nib<Word, RPL>(FV[k], g);
-                            const int j1 = two ? nib<Word, RPL>(FV[k], g + 1) + 16 : j0;
-                            const Word m = two ? ~(Word)0 : (Word)0;
-                            fD[k] ^= TF[j0] ^ (TF[j1] & m);
-                            yP[k] ^= TP[j0] ^ (TP[j1] & m);
-                            Y[k] ^= TK[j0] ^ (TK[j1] & m);
+                            const Word* e0 = T + (g * 16 + nib<Word, RPL>(FV[k], g)) * 3;
+                            const Word* e1 = T + ((g + 1) * 16 + nib<Word, RPL>(FV[k], g + 1)) * 3;
+                            fD[k] ^= e0[0] ^ e1[0];
+                            yP[k] ^= e0[1] ^ e1[1];
+                            Y[k] ^= e0[2] ^ e1[2];
                         }
                     }
                 }
 #pragma unroll (UNROLL_BRA / 2 > 0 ? UNROLL_BRA / 2 : 1)
                 for (int g = 0; g < GMAX; g += 2) {
                     if (g < ngrp) {
-                        const bool two = g + 1 < ngrp;
-                        const Word m = two ? ~(Word)0 : (Word)0;
 #pragma unroll
                         for (int k = 0; k < RPL; k++) {
                             const int j0 = g * 16 + nib<Word, RPL>(Y[k], g);
-                            const int j1 = two ? (g + 1) * 16 + nib<Word, RPL>(Y[k], g + 1) : j0;
-                            Kr[k] ^= tbA[j0] ^ (tbA[j1] & m);
+                            const int j1 = (g + 1) * 16 + nib<Word, RPL>(Y[k], g + 1);
+                            Kr[k] ^= tbA[j0] ^ tbA[j1];
                         }
                     }
                 }
@@ -807,7 +811,7 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                 for (int k = 0; k < RPL; k++) {
                     J[k] = Lw[k] | LwT[k];
                     sF[32 * k + lane] = fD[k];
-                    sJ[32 * k + lane] = J[k];
+                    sJ[32 * k + lane] = (J[k] & vA) | (Lw[k] & ~vA);
                 }
                 __syncwarp();
 
@@ -821,18 +825,15 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                 for (int g = 0; g < NG; g++) {
                     const Word x = xs[g], xf = x & ~vA & full;
                     const int gx = popc<Word>(xf & g0) + 2 * popc<Word>(xf & g1);
-                    int qx = 0;
-                    Word xF = 0, Jx = 0, t = xf;
+                    Word xF = 0, Mx = 0, t = xf;
                     while (t) {
                         const int q = ffs0<Word>(t);
                         t &= t - 1;
-                        const Word Jq = sJ[q];
-                        qx ^= parity<Word>(Jq & xf & (((Word)1 << q) - 1)) ^ (int)((diag >> q) & 1);
                         xF ^= sF[q];
-                        Jx ^= Jq;
+                        Mx ^= sJ[q];
                     }
-                    ph[g] = phB + 2 * gx + 4 * (qx ^ parity<Word>(xF & w));
-                    h[g] = (x ^ Jx) & vA;
+                    ph[g] = phB + 2 * gx + 4 * parity<Word>(((Mx ^ diag) & xf) ^ (xF & w));
+                    h[g] = (x ^ Mx) & vA;
                     rhs[g] = (sB ^ xF) & cons;
                     zero[g] = false;
                 }
@@ -861,8 +862,8 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         for (int g = 0; g < NG; g++) zero[g] |= c[g];
                         continue;
                     }
-                    const int kq = ffs0<Word>(l);
-                    const Word lp = l & (l - 1);
+                    const int kq = sizeof(Word) == 8 ? fls0<Word>(l) : ffs0<Word>(l);
+                    const Word lp = l ^ ((Word)1 << kq);
                     const Word Fk = row_of<Word, RPL>(Fc, kq);
 #pragma unroll
                     for (int k = 0; k < RPL; k++)
@@ -1438,7 +1439,7 @@ size_t ket_table_ket_bytes(int n) { return (size_t)3 * ket_table_groups(n) * 16 
 
 size_t ket_table_bra_bytes(int n) { return (size_t)ket_table_groups(n) * 16 * pair_word_bytes(n); }
 
-int ket_table_groups(int n) { return n <= 0 ? 1 : (n + 3) / 4; }
+int ket_table_groups(int n) { return n <= 0 ? 2 : ((n + 3) / 4 + 1) & ~1; }
 
 cudaError_t launch_ket_tables(const TermsView& t, void* out, cudaStream_t st) {
     if (t.chi == 0) return cudaSuccess;
