@@ -272,7 +272,8 @@ struct ChunkAcc {
 //   K        K[c][r] = parity(M_c·F_r), i.e. K = M·F^T,
 // then a 48-byte trailer with the term's scalars (KetTrailer), and last the
 // table of G, which the pair kernel reads when the term is the bra.  Layout
-// per term: [F|P|K][ngrp][16] Words, trailer, [G][ngrp][16] Words; one bulk
+// per term: [ngrp][16][F, P, K] Words (the three entries of one index side
+// by side, so one address serves three loads), trailer, [G][ngrp][16] Words; one bulk
 // copy of the first part brings everything the kernel reads of a ket.  ngrp
 // is ⌈n/4⌉ rounded up to an even count: the padding group is all zeros, so
 // the pair kernel looks groups up two at a time with no mask.
@@ -1431,7 +1432,7 @@ cudaError_t launch_pauli_frames(const TermsView& t, const DevPauli* d_paulis, in
 
 static int pair_word_bytes(int n) { return n <= 32 ? 4 : 8; }
 
-size_t ket_table_stride(int n) {  // bytes per term: [F|P|K][ngrp][16] words, trailer, [G][ngrp][16] words
+size_t ket_table_stride(int n) {  // bytes per term: [ngrp][16][F, P, K] words, trailer, [G][ngrp][16] words
     return (size_t)4 * ket_table_groups(n) * 16 * pair_word_bytes(n) + sizeof(KetTrailer);
 }
 
