@@ -35,6 +35,7 @@
 #include <map>
 #include <mutex>
 #include <tuple>
+#include <type_traits>
 
 #include "device_state.hpp"
 #include "warp_chform.cuh"
@@ -458,12 +459,30 @@ __device__ __forceinline__ void g_expand(Word (&J)[RPL], Word& hs, Word& L0, Wor
     L0 ^= T;
 }
 
-// subst: eliminate z_k = c ⊕ lp·z (c per observable) from the form.
-template <typename Word, int RPL, int NG>
-__device__ __forceinline__ void g_subst(int kq, Word lp, const bool (&c)[NG], Word (&J)[RPL], Word& hs, Word& L0,
+// Calls f(slot, q) for the highest (HIGHEST) or lowest set bit of m ≠ 0:
+// slot (a std::integral_constant) is the row slot that holds that row, q its
+// bit within the slot's 32 bits.  Knowing the slot at compile time lets every
+// test and update on that bit run on the one 32-bit half that holds it.
+template <typename Word, bool HIGHEST, typename F>
+__device__ __forceinline__ void on_bit(Word m, F&& f) {
+    if constexpr (sizeof(Word) == 8) {
+        const uint32_t hi = (uint32_t)((uint64_t)m >> 32), lo = (uint32_t)m;
+        if (HIGHEST ? hi != 0 : lo == 0)
+            f(std::integral_constant<int, 1>{}, HIGHEST ? 31 - __clz(hi) : __ffs(hi) - 1);
+        else
+            f(std::integral_constant<int, 0>{}, HIGHEST ? 31 - __clz(lo) : __ffs(lo) - 1);
+    } else {
+        f(std::integral_constant<int, 0>{}, HIGHEST ? 31 - __clz((uint32_t)m) : __ffs((uint32_t)m) - 1);
+    }
+}
+
+// subst: eliminate z_k = c ⊕ lp·z (c per observable) from the form; k is
+// bit q of row slot H (k = 32·H + q).
+template <typename Word, int RPL, int NG, int H>
+__device__ __forceinline__ void g_subst(int q, Word lp, const bool (&c)[NG], Word (&J)[RPL], Word& hs, Word& L0,
                                         Word& alive, Word (&h)[NG], int (&ph)[NG], const Word (&own)[RPL]) {
-    const Word kb = (Word)1 << kq;
-    const Word R = row_of<Word, RPL>(J, kq) & alive & ~kb;
+    const Word kb = (Word)(1u << q) << (32 * H);
+    const Word R = shfl<Word>(J[H], q) & alive & ~kb;
 #pragma unroll
     for (int k = 0; k < RPL; k++) {  // z_k·(R·z) → (lp·z)(R·z): J ^= lp·Rᵀ + R·lpᵀ
         const uint32_t lbit = (uint32_t)own[0];
@@ -494,8 +513,6 @@ template <typename Word>
 __device__ __forceinline__ int fls0(Word x);  // index of the highest set bit
 template <>
 __device__ __forceinline__ int fls0<uint32_t>(uint32_t x) { return 31 - __clz(x); }
-template <>
-__device__ __forceinline__ int fls0<uint64_t>(uint64_t x) { return 63 - __clzll((long long)x); }
 
 // Sums out alive variables while one is left in `until` (the summation rounds
 // of the pair kernel).  A variable removed from `alive` keeps its bits of hs,
@@ -553,8 +570,10 @@ __device__ __forceinline__ void sum_out(Word (&J)[RPL], Word& hs, Word& L0, Word
             const bool hsj = (hs & jb) != 0;
 #pragma unroll
             for (int g = 0; g < NG; g++) hb[g] = hsj ^ ((h[g] & jb) != 0);
-            const int kq = HIGH ? fls0<Word>(S) : ffs0<Word>(S);
-            g_subst<Word, RPL, NG>(kq, S ^ ((Word)1 << kq), hb, J, hs, L0, alive, h, ph, own);
+            on_bit<Word, HIGH>(S, [&](auto slot, int q) {
+                constexpr int H = decltype(slot)::value;
+                g_subst<Word, RPL, NG, H>(q, S ^ ((Word)(1u << q) << (32 * H)), hb, J, hs, L0, alive, h, ph, own);
+            });
         }
     }
 }
@@ -863,16 +882,18 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         for (int g = 0; g < NG; g++) zero[g] |= c[g];
                         continue;
                     }
-                    const int kq = sizeof(Word) == 8 ? fls0<Word>(l) : ffs0<Word>(l);
-                    const Word lp = l ^ ((Word)1 << kq);
-                    const Word Fk = row_of<Word, RPL>(Fc, kq);
+                    on_bit<Word, sizeof(Word) == 8>(l, [&](auto slot, int q) {
+                        constexpr int H = decltype(slot)::value;
+                        const Word lp = l ^ ((Word)(1u << q) << (32 * H));
+                        const Word Fk = shfl<Word>(Fc[H], q);
 #pragma unroll
-                    for (int k = 0; k < RPL; k++)
-                        if (own_bit<Word>(lp, k, (uint32_t)own[0])) Fc[k] ^= Fk;
+                        for (int k = 0; k < RPL; k++)
+                            if (own_bit<Word>(lp, k, (uint32_t)own[0])) Fc[k] ^= Fk;
 #pragma unroll
-                    for (int g = 0; g < NG; g++)
-                        if (c[g]) rhs[g] ^= Fk;
-                    g_subst<Word, RPL, NG>(kq, lp, c, J, hs, L0, alive, h, ph, own);
+                        for (int g = 0; g < NG; g++)
+                            if (c[g]) rhs[g] ^= Fk;
+                        g_subst<Word, RPL, NG, H>(q, lp, c, J, hs, L0, alive, h, ph, own);
+                    });
                 }
                 // summation (sum_out)
                 Word IE = 0, IO = 0;
