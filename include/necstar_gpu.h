@@ -257,7 +257,8 @@ nsg_status nsg_exp_value_noalloc(const nsg_state* state, const nsg_pauli* pauli,
  * operation that changes a state's rank, width or global factor (projection,
  * discard, measurement) or frees it makes nsg_plan_run fail with
  * NSG_ERR_INVALID_ARGUMENT.  Creation picks, for each row width, the
- * pair-kernel variant (2-5 blocks per SM), the tasks per resident warp (16,
+ * pair-kernel variant (2-6 blocks per SM for 32-bit rows, 2-5 for 64-bit
+ * rows), the tasks per resident warp (16,
  * 64, 256) and the kets per chunk (16, 32, 64), in that order, by timing the
  * candidates on the plan's own work (whole launches when short, else the
  * first two tasks per resident warp); the choice is remembered per device

@@ -644,7 +644,10 @@ struct TuneChoice {
 std::mutex g_tune_mu;
 std::map<std::string, TuneChoice> g_tune;
 bool g_tune_loaded = false;
-constexpr int kMinbCandidates[4] = {2, 3, 4, 5};
+constexpr int kMinbCandidates[5] = {2, 3, 4, 5, 6};
+// The most blocks per SM a variant of that row width has: six only for 32-bit
+// rows (64-bit rows would spill at the 85 registers six blocks leave).
+int max_minb(int wb) { return wb == 4 ? 6 : 5; }
 constexpr int kTpwCandidates[3] = {16, 64, 256};
 // Task records of one launch stay below this (tasks × observables × 64 B); a
 // launch with many observables gets fewer, longer tasks.
@@ -690,7 +693,7 @@ void tune_load_locked() {
         TuneChoice c;
         const int got = std::sscanf(line, " {\"key\": \"%255[^\"]\", \"minb\": %d, \"tasks_per_warp\": %d, \"chunk\": %d}",
                                     key, &c.minb, &c.tasks_per_warp, &c.chunk);
-        if (got >= 2 && c.minb >= 2 && c.minb <= 5 && c.tasks_per_warp >= 1 && c.tasks_per_warp <= 1024 &&
+        if (got >= 2 && c.minb >= 2 && c.minb <= 6 && c.tasks_per_warp >= 1 && c.tasks_per_warp <= 1024 &&
             c.chunk >= 1 && c.chunk <= 1024)
             g_tune[key] = c;  // a line without the last two fields keeps their defaults
     }
@@ -721,11 +724,12 @@ void tune_store(const std::string& key, const TuneChoice& c) {
 
 // The pair-kernel variant when nothing was tuned for a workload class, from
 // full-launch timings on GB300 (χ = 972 at n = 28 and 40, χ = 2916 at n = 60;
-// 1, 64 and 256 observables): five blocks per SM for 32-bit rows; for 64-bit
-// rows four up to n = 48, beyond that three, or two with more than 128
-// observables (their per-lane state needs the registers).
+// 1, 64 and 256 observables; six blocks for 32-bit rows from the 512-circuit
+// workload): six blocks per SM for 32-bit rows; for 64-bit rows four up to
+// n = 48, beyond that three, or two with more than 128 observables (their
+// per-lane state needs the registers).
 int default_minb(int wb, int nobs_max, int n_mean) {
-    if (wb == 4) return 5;
+    if (wb == 4) return 6;
     if (n_mean <= 48) return 4;
     return nobs_max > 128 ? 2 : 3;
 }
@@ -851,7 +855,7 @@ void build_batch(PairBatch& b, const PairTiling& tl, bool mixed, cudaStream_t st
             const int n_mean = pairs ? (int)(nsum / pairs) : 0;
             TuneChoice c;
             const bool hit = tune_lookup(tune_key(dev, wb, nobs_max, n_mean, pairs), c);
-            if (minb == 0) minb = hit ? c.minb : default_minb(wb, nobs_max, n_mean);
+            if (minb == 0) minb = hit ? std::min(c.minb, max_minb(wb)) : default_minb(wb, nobs_max, n_mean);
             if (tpw == 0) tpw = hit ? c.tasks_per_warp : TuneChoice().tasks_per_warp;
             if (chunk == 0) chunk = hit ? c.chunk : TuneChoice().chunk;
         }
@@ -2095,9 +2099,11 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
             auto stage = [&](int field, const int* vals, int nvals) {
                 for (int v = 0; v < nvals; v++) {
                     PairTiling tc = tl;
-                    bool any = false;
+                    bool any = false, on[2] = {false, false};
                     for (int idx = 0; idx < 2; idx++) {
                         if (!need_time[idx]) continue;
+                        if (field == 0 && vals[v] > max_minb(idx == 0 ? 4 : 8)) continue;
+                        on[idx] = true;
                         TuneChoice c = best[idx];
                         if (c.minb == 0) c.minb = 4;
                         if (field == 0) c.minb = vals[v];
@@ -2108,7 +2114,7 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
                         tc.chunk[idx] = c.chunk;
                         any = true;
                     }
-                    if (!any) return;
+                    if (!any) continue;
                     PairBatch b;
                     plan->build(b, tc, mixed, true);
                     for (size_t k = 0; k < b.live.size(); k++)
@@ -2116,7 +2122,7 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
                                                b.px.p + b.unit_px[k], b.pk.p + b.unit_px[k], st));
                     for (size_t li = 0; li < b.launches.size(); li++) {
                         const int idx = b.launches[li].wb == 4 ? 0 : 1;
-                        if (!need_time[idx]) continue;
+                        if (!need_time[idx] || !on[idx]) continue;
                         sample_ns_per_pair(b, li, st, 1);  // first launch of the candidate: warm-up
                         const double ns = sample_ns_per_pair(b, li, st, rounds[idx]);
                         if (ns < best_ns[idx]) {
@@ -2140,7 +2146,7 @@ nsg_status nsg_plan_create(const nsg_state* const* states, size_t num_states, co
                     tl.tasks_per_warp[idx] = TuneChoice().tasks_per_warp;
                     tl.chunk[idx] = TuneChoice().chunk;
                 }
-            stage(0, kMinbCandidates, 4);
+            stage(0, kMinbCandidates, 5);
             stage(1, kTpwCandidates, 3);
             stage(2, kChunkCandidates, 3);
             for (int idx = 0; idx < 2; idx++)

@@ -1358,6 +1358,9 @@ cudaError_t launch_pairs_minb(const MultiLaunch& p, cudaStream_t st) {
         case 2: return launch_pairs_ng<Word, RPL, NG, 2>(p, st);
         case 3: return launch_pairs_ng<Word, RPL, NG, 3>(p, st);
         case 5: return launch_pairs_ng<Word, RPL, NG, 5>(p, st);
+        case 6:  // 32-bit rows only (the host caps 64-bit rows at five)
+            if constexpr (sizeof(Word) == 4) return launch_pairs_ng<Word, RPL, NG, 6>(p, st);
+            else return launch_pairs_ng<Word, RPL, NG, 5>(p, st);
         default: return launch_pairs_ng<Word, RPL, NG, 4>(p, st);
     }
 }
@@ -1379,6 +1382,9 @@ int resident_blocks_minb(size_t warp_smem, int minb) {
         case 2: return resident_blocks_ng<Word, RPL, NG, 2>(warp_smem);
         case 3: return resident_blocks_ng<Word, RPL, NG, 3>(warp_smem);
         case 5: return resident_blocks_ng<Word, RPL, NG, 5>(warp_smem);
+        case 6:
+            if constexpr (sizeof(Word) == 4) return resident_blocks_ng<Word, RPL, NG, 6>(warp_smem);
+            else return resident_blocks_ng<Word, RPL, NG, 5>(warp_smem);
         default: return resident_blocks_ng<Word, RPL, NG, 4>(warp_smem);
     }
 }

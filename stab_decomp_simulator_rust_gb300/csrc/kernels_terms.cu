@@ -23,8 +23,8 @@ constexpr int kCompileWarps = 4;  // warps per block of the compile kernel
 // A warp-held term with W 64-bit words per row in RPL row slots of 32 rows
 // (RPL = 2W holds every row of the storage; the compile kernel uses RPL = 3
 // for widths 65-96).
-template <int W, int RPL = 2 * W>
-using Eng = WarpCH<uint64_t, W, RPL>;
+template <int W, int RPL = 2 * W, typename Word = uint64_t>
+using Eng = WarpCH<Word, W, RPL>;
 
 // ---- load / store a term between HBM (any storage W) and a warp engine -----
 template <int W, int RPL = 2 * W>
@@ -59,6 +59,103 @@ __device__ __forceinline__ void load_term(Eng<W, RPL>& e, const TermsView& tv, i
     for (int w = 0; w < W; w++) {
         e.v.w[w] = (w < tv.W) ? tv.V[(size_t)term * tv.W + w] : 0;
         e.s.w[w] = (w < tv.W) ? tv.S[(size_t)term * tv.W + w] : 0;
+    }
+}
+
+// A term held as 32-bit words (two per storage word).
+template <int W, int RPL>
+__device__ __forceinline__ void load_term(Eng<W, RPL, uint32_t>& e, const TermsView& tv, int64_t term) {
+    e.n = tv.n;
+    e.err = 0;
+    e.phase = tv.phase[term];
+    e.gam = 0;
+#pragma unroll
+    for (int k = 0; k < RPL; k++) {
+        int r = 32 * k + e.lane;
+#pragma unroll
+        for (int sw = 0; 2 * sw < W; sw++) {
+            uint64_t g = 0, f = 0, m = 0;
+            if (r < tv.R && sw < tv.W) {
+                size_t idx = ((size_t)term * tv.R + r) * tv.W + sw;
+                g = tv.G[idx];
+                f = tv.F[idx];
+                m = tv.M[idx];
+            }
+            e.G[k].w[2 * sw] = (uint32_t)g;
+            e.F[k].w[2 * sw] = (uint32_t)f;
+            e.M[k].w[2 * sw] = (uint32_t)m;
+            if (2 * sw + 1 < W) {
+                e.G[k].w[2 * sw + 1] = (uint32_t)(g >> 32);
+                e.F[k].w[2 * sw + 1] = (uint32_t)(f >> 32);
+                e.M[k].w[2 * sw + 1] = (uint32_t)(m >> 32);
+            }
+        }
+        int gw = r >> 6;
+        uint64_t gl = (gw < tv.W) ? tv.GL[(size_t)term * tv.W + gw] : 0;
+        uint64_t gh = (gw < tv.W) ? tv.GH[(size_t)term * tv.W + gw] : 0;
+        int g = (int)((gl >> (r & 63)) & 1) | ((int)((gh >> (r & 63)) & 1) << 1);
+        e.gam_set(k, g);
+    }
+#pragma unroll
+    for (int sw = 0; 2 * sw < W; sw++) {
+        const uint64_t vv = (sw < tv.W) ? tv.V[(size_t)term * tv.W + sw] : 0;
+        const uint64_t ss = (sw < tv.W) ? tv.S[(size_t)term * tv.W + sw] : 0;
+        e.v.w[2 * sw] = (uint32_t)vv;
+        e.s.w[2 * sw] = (uint32_t)ss;
+        if (2 * sw + 1 < W) {
+            e.v.w[2 * sw + 1] = (uint32_t)(vv >> 32);
+            e.s.w[2 * sw + 1] = (uint32_t)(ss >> 32);
+        }
+    }
+}
+
+// The storage word w of a row held as 32-bit words (two of them per word).
+template <int W>
+__device__ __forceinline__ uint64_t storage_word(const BV<uint32_t, W>& x, int w) {
+    const uint32_t lo = (2 * w < W) ? x.w[(2 * w < W) ? 2 * w : 0] : 0u;
+    const uint32_t hi = (2 * w + 1 < W) ? x.w[(2 * w + 1 < W) ? 2 * w + 1 : 0] : 0u;
+    return (uint64_t)lo | ((uint64_t)hi << 32);
+}
+
+template <int W, int RPL>
+__device__ __forceinline__ void store_term(const Eng<W, RPL, uint32_t>& e, const TermsView& tv, int64_t term) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {  // every row slot of the storage; slots the engine does not hold are zero
+        int r = 32 * k + e.lane;
+        if (r < tv.R) {
+#pragma unroll
+            for (int w = 0; w < 2; w++) {
+                if (w < tv.W) {
+                    const bool held = k < RPL;
+                    const int kk = k < RPL ? k : 0;
+                    size_t idx = ((size_t)term * tv.R + r) * tv.W + w;
+                    tv.G[idx] = held ? storage_word<W>(e.G[kk], w) : 0;
+                    tv.F[idx] = held ? storage_word<W>(e.F[kk], w) : 0;
+                    tv.M[idx] = held ? storage_word<W>(e.M[kk], w) : 0;
+                }
+            }
+        }
+    }
+    uint64_t gl[2] = {0, 0}, gh[2] = {0, 0};
+#pragma unroll
+    for (int k = 0; k < RPL; k++) {
+        int g = e.gam_of(k);
+        uint32_t b0 = __ballot_sync(dev::FULL, g & 1);
+        uint32_t b1 = __ballot_sync(dev::FULL, (g >> 1) & 1);
+        gl[k >> 1] |= (uint64_t)b0 << (32 * (k & 1));
+        gh[k >> 1] |= (uint64_t)b1 << (32 * (k & 1));
+    }
+    if (e.lane == 0) {
+#pragma unroll
+        for (int w = 0; w < 2; w++) {
+            if (w < tv.W) {
+                tv.GL[(size_t)term * tv.W + w] = gl[w];
+                tv.GH[(size_t)term * tv.W + w] = gh[w];
+                tv.V[(size_t)term * tv.W + w] = storage_word<W>(e.v, w);
+                tv.S[(size_t)term * tv.W + w] = storage_word<W>(e.s, w);
+            }
+        }
+        tv.phase[term] = (uint8_t)e.phase;
     }
 }
 
@@ -105,8 +202,8 @@ __device__ __forceinline__ void store_term(const Eng<W, RPL>& e, const TermsView
     }
 }
 
-template <int W, int RPL = 2 * W>
-__device__ __forceinline__ void apply_prim(Eng<W, RPL>& e, uint32_t code) {
+template <int W, int RPL = 2 * W, typename Word = uint64_t>
+__device__ __forceinline__ void apply_prim(Eng<W, RPL, Word>& e, uint32_t code) {
     uint32_t op = code & 0xff, a = (code >> 8) & 0xff, b = (code >> 16) & 0xff;
     switch (op) {
         case P_H: e.left_h(a); break;
@@ -124,7 +221,7 @@ __device__ __forceinline__ void apply_prim(Eng<W, RPL>& e, uint32_t code) {
 // ---- compile ------------------------------------------------------------------
 // CW warps per block: a compile launch has one warp per T-term, often only a few
 // per SM, so small blocks spread them evenly over the SMs.
-template <int W, int RPL, int CW>
+template <int W, int RPL, int CW, typename Word = uint64_t>
 __global__ void __launch_bounds__(CW * 32) compile_kernel(
     const uint32_t* __restrict__ ops, int nops, int n, int t, int64_t chi_t,
     const uint64_t* __restrict__ tG, const uint64_t* __restrict__ tF, const uint64_t* __restrict__ tM,
@@ -137,7 +234,8 @@ __global__ void __launch_bounds__(CW * 32) compile_kernel(
     const bool active = term < chi_t;
     const int width = n + t;
 
-    Eng<W, RPL> e;
+    Eng<W, RPL, Word> e;
+    constexpr int WB = 8 * (int)sizeof(Word);
     e.lane = lane;
     e.init_zero(width);
     if (active) {
@@ -148,16 +246,16 @@ __global__ void __launch_bounds__(CW * 32) compile_kernel(
             if (r >= n && r < width) {
                 int tr = r - n;
                 size_t idx = (size_t)term * t + tr;
-                BV<uint64_t, W> g = BV<uint64_t, W>::zero(), f = g, m = g;
+                BV<Word, W> g = BV<Word, W>::zero(), f = g, m = g;
                 uint64_t gw = tG[idx], fw = tF[idx], mw = tM[idx];
 #pragma unroll
                 for (int w = 0; w < W; w++) {
-                    int lo = 64 * w;
+                    int lo = WB * w;
                     // bit c of the shifted row = bit (c - n) of the T row
-                    auto sh = [&](uint64_t x) -> uint64_t {
+                    auto sh = [&](uint64_t x) -> Word {
                         int off = lo - n;  // T bit index of this word's bit 0
-                        if (off >= 64 || off <= -64) return 0;
-                        return off >= 0 ? (x >> off) : (x << (-off));
+                        if (off >= 64 || off <= -WB) return 0;
+                        return (Word)(off >= 0 ? (x >> off) : (x << (-off)));
                     };
                     g.w[w] = sh(gw);
                     f.w[w] = sh(fw);
@@ -172,9 +270,9 @@ __global__ void __launch_bounds__(CW * 32) compile_kernel(
         uint64_t vv = tV[term], ss = tS[term];
 #pragma unroll
         for (int w = 0; w < W; w++) {
-            int off = 64 * w - n;
-            e.v.w[w] = (off >= 64 || off <= -64) ? 0 : (off >= 0 ? (vv >> off) : (vv << (-off)));
-            e.s.w[w] = (off >= 64 || off <= -64) ? 0 : (off >= 0 ? (ss >> off) : (ss << (-off)));
+            int off = WB * w - n;
+            e.v.w[w] = (off >= 64 || off <= -WB) ? (Word)0 : (Word)(off >= 0 ? (vv >> off) : (vv << (-off)));
+            e.s.w[w] = (off >= 64 || off <= -WB) ? (Word)0 : (Word)(off >= 0 ? (ss >> off) : (ss << (-off)));
         }
         e.phase = tPhase[term];
     }
@@ -185,7 +283,7 @@ __global__ void __launch_bounds__(CW * 32) compile_kernel(
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) sops[i] = ops[base + i];
         __syncthreads();
         if (active && !e.err) {
-            for (int i = 0; i < cnt; i++) apply_prim<W, RPL>(e, sops[i]);
+            for (int i = 0; i < cnt; i++) apply_prim<W, RPL, Word>(e, sops[i]);
         }
     }
     if (!active) return;
@@ -393,20 +491,20 @@ __global__ void __launch_bounds__(WARPS * 32) apply_ops_kernel(const uint32_t* _
     __shared__ uint32_t sops[OPS_CHUNK];
     const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     const bool active = term < tv.chi;
-    Eng<W> e;
+    Eng<2 * W, 2 * W, uint32_t> e;  // 32-bit words
     e.lane = threadIdx.x & 31;
-    if (active) load_term<W>(e, tv, term);
+    if (active) load_term(e, tv, term);
     for (int base = 0; base < nops; base += OPS_CHUNK) {
         int cnt = min(OPS_CHUNK, nops - base);
         __syncthreads();
         for (int i = threadIdx.x; i < cnt; i += blockDim.x) sops[i] = ops[base + i];
         __syncthreads();
         if (active && !e.err)
-            for (int i = 0; i < cnt; i++) apply_prim<W>(e, sops[i]);
+            for (int i = 0; i < cnt; i++) apply_prim<2 * W, 2 * W, uint32_t>(e, sops[i]);
     }
     if (!active) return;
     if (e.err && e.lane == 0) atomicOr(status, DS_INVARIANT);
-    store_term<W>(e, tv, term);
+    store_term(e, tv, term);
 }
 
 template <int W>
@@ -414,9 +512,9 @@ __global__ void __launch_bounds__(WARPS * 32) project_kernel(TermsView tv, int q
                                                             int32_t* __restrict__ keep, int* __restrict__ status) {
     const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (term >= tv.chi) return;
-    Eng<W> e;
+    Eng<2 * W, 2 * W, uint32_t> e;  // 32-bit words
     e.lane = threadIdx.x & 31;
-    load_term<W>(e, tv, term);
+    load_term(e, tv, term);
     int r = e.project(q, outcome != 0);
     if (e.err) {
         if (e.lane == 0) atomicOr(status, DS_INVARIANT);
@@ -426,19 +524,19 @@ __global__ void __launch_bounds__(WARPS * 32) project_kernel(TermsView tv, int q
         keep[term] = (r >= 0) ? 1 : 0;
         if (r == 0) tv.coef_r[term] += 1;  // amplify(-1): r -= -1 (projection.rs:44)
     }
-    if (r == 0) store_term<W>(e, tv, term);
+    if (r == 0) store_term(e, tv, term);
 }
 
 template <int W>
 __global__ void __launch_bounds__(WARPS * 32) discard_kernel(TermsView tv, int q, int* __restrict__ status) {
     const int64_t term = (int64_t)blockIdx.x * WARPS + (threadIdx.x >> 5);
     if (term >= tv.chi) return;
-    Eng<W> e;
+    Eng<2 * W, 2 * W, uint32_t> e;  // 32-bit words
     e.lane = threadIdx.x & 31;
-    load_term<W>(e, tv, term);
+    load_term(e, tv, term);
     e.discard(q);
     if (e.err && e.lane == 0) atomicOr(status, e.err == 2 ? DS_CANNOT_DISCARD : DS_INVARIANT);
-    store_term<W>(e, tv, term);  // width n-1 in the same storage
+    store_term(e, tv, term);  // width n-1 in the same storage
 }
 
 // ---- pack / unpack bool bytes -------------------------------------------------
@@ -563,13 +661,13 @@ cudaError_t launch_compile(const uint32_t* d_ops, int nops, int n, int t, int64_
     constexpr int CW = kCompileWarps;
     dim3 grid((unsigned)((chi_t + CW - 1) / CW)), block(CW * 32);
     if (width <= 64)
-        compile_kernel<1, 2, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
+        compile_kernel<2, 2, CW, uint32_t><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
                                                          tCk, tCr, out, keep, status);
-    else if (width <= 96)  // three row slots: a quarter less work than the full 128 rows
-        compile_kernel<2, 3, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
+    else if (width <= 96)  // three row slots of three 32-bit words: 96 rows of 96 columns
+        compile_kernel<3, 3, CW, uint32_t><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
                                                          tCk, tCr, out, keep, status);
     else
-        compile_kernel<2, 4, CW><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
+        compile_kernel<4, 4, CW, uint32_t><<<grid, block, 0, st>>>(d_ops, nops, n, t, chi_t, tG, tF, tM, tGam, tV, tS, tPhase,
                                                          tCk, tCr, out, keep, status);
     return cudaGetLastError();
 }

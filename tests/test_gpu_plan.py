@@ -52,7 +52,7 @@ def test_plan_matches_direct_and_oracle(gpu_pkg, oracle, precision):
             assert abs(got[c][o] - ex) <= TOL * max(1.0, abs(ex)), (c, o)
     t = plan.tiling
     for w in ("rows32", "rows64"):  # SPECS has states of both row widths
-        assert t[f"minb_{w}"] in (2, 3, 4, 5)
+        assert t[f"minb_{w}"] in ((2, 3, 4, 5, 6) if w == "rows32" else (2, 3, 4, 5))
         assert t[f"chunk_{w}"] in (16, 32, 64) and t[f"tasks_per_warp_{w}"] in (16, 64, 256)
 
 
