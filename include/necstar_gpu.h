@@ -188,7 +188,11 @@ nsg_status nsg_state_set_stream(nsg_state* state, void* cuda_stream);
 
 /* QuantumState::apply_gates (crates/necstar/src/state/mod.rs:522-526 →
  * stabilizer_decomposed_state/gates.rs:7-37); T/Tdg/CCX give
- * NSG_ERR_NON_CLIFFORD_GATE_APPLICATION. */
+ * NSG_ERR_NON_CLIFFORD_GATE_APPLICATION.  A list that lowers to at most eight
+ * primitive gates without H (one S, Sdg, X, Y, Z, CX, CZ or SWAP gate, for
+ * instance) is applied by one thread per term to the rows it touches and the
+ * call returns without waiting for the device; other lists run one warp per
+ * term over the whole gate list and wait for its status. */
 nsg_status nsg_apply_gates(nsg_state* state, const nsg_gate* gates, size_t num_gates);
 
 /* ------------------------------------------------------------------------ */

@@ -1209,6 +1209,19 @@ void discard_q(nsg_state* s, uint32_t q) {  // discard.rs:5-12
 
 void apply_ops(nsg_state* s, const std::vector<uint32_t>& ops) {
     if (ops.empty() || s->t.chi == 0) return;
+    // A few gates without H (one gate of a gate-by-gate caller, mostly): one
+    // thread per term updates the rows they touch; nothing to allocate or
+    // check, so the call does not wait for the device.
+    bool row_only = ops.size() <= (size_t)kRowOpsMax;
+    for (uint32_t c : ops) row_only = row_only && (c & 0xff) != P_H;
+    if (row_only) {
+        RowOps r{};
+        r.n = (int)ops.size();
+        for (size_t i = 0; i < ops.size(); i++) r.code[i] = ops[i];
+        CK(launch_row_ops(r, s->t.view(), s->st));
+        s->invalidate();
+        return;
+    }
     DBuf<uint32_t> d;
     d.alloc(ops.size(), s->st);
     CK(cudaMemcpyAsync(d.p, ops.data(), ops.size() * 4, cudaMemcpyHostToDevice, s->st));

@@ -124,6 +124,16 @@ cudaError_t launch_compact(const TermsView& in, const int32_t* keep, int32_t* sc
 cudaError_t launch_apply_ops(const uint32_t* d_ops, int nops, TermsView terms, int* status,
                              cudaStream_t st);
 
+// A short list of primitive ops without H (S, Sdg, Z, X, Y, CZ, CX), passed by
+// value: one thread per term updates only the rows the ops touch.  These
+// updates cannot fail, so there is no status word.
+constexpr int kRowOpsMax = 8;
+struct RowOps {
+    int n;
+    uint32_t code[kRowOpsMax];
+};
+cudaError_t launch_row_ops(const RowOps& ops, TermsView terms, cudaStream_t st);
+
 // Project every term on (qubit, outcome): keep[i] = 0 if impossible; the
 // coefficient is amplified by -1 for random outcomes (projection.rs:27-57).
 cudaError_t launch_project(TermsView terms, int qubit, int outcome, int32_t* keep, int* status,

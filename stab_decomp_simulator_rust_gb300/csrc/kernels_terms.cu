@@ -507,6 +507,80 @@ __global__ void __launch_bounds__(WARPS * 32) apply_ops_kernel(const uint32_t* _
     store_term(e, tv, term);
 }
 
+// ---- short runs of gates without H, one thread per term ----------------------
+// S, Sdg, Z, X, Y, CZ and CX each change a few rows of a term (the left
+// multiplication rules of form/left_multiplication/{s,z,x,y,cz,cx}.rs, the same
+// updates as WarpCH's left_*), so a call with a few of them reads and writes
+// only those rows in place instead of moving every term through a warp: an S
+// gate touches 3·8W + 2 bytes of a term, not the whole tableau.
+template <int W>
+__global__ void __launch_bounds__(256) row_ops_kernel(TermsView tv, RowOps ops) {
+    const int64_t term = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (term >= tv.chi) return;
+    const size_t rb = (size_t)term * tv.R;
+    auto at = [&](uint32_t r, int w) -> size_t { return (rb + r) * W + w; };
+    auto gam = [&](uint32_t q) -> int {
+        const size_t o = (size_t)term * W + (q >> 6);
+        return (int)((tv.GL[o] >> (q & 63)) & 1) | ((int)((tv.GH[o] >> (q & 63)) & 1) << 1);
+    };
+    auto set_gam = [&](uint32_t q, int g) {
+        const size_t o = (size_t)term * W + (q >> 6);
+        const uint64_t bit = 1ull << (q & 63);
+        tv.GL[o] = (g & 1) ? (tv.GL[o] | bit) : (tv.GL[o] & ~bit);
+        tv.GH[o] = (g & 2) ? (tv.GH[o] | bit) : (tv.GH[o] & ~bit);
+    };
+    int phase = tv.phase[term];
+    for (int i = 0; i < ops.n; i++) {
+        const uint32_t code = ops.code[i], op = code & 0xff, a = (code >> 8) & 0xff, b = (code >> 16) & 0xff;
+        switch (op) {
+            case P_S:
+            case P_SDG:  // M[a] ^= G[a]; γ_a -= 1 (S) or += 1 (Sdg)
+#pragma unroll
+                for (int w = 0; w < W; w++) tv.M[at(a, w)] ^= tv.G[at(a, w)];
+                set_gam(a, gam(a) + (op == P_S ? 3 : 1));
+                break;
+            case P_Z: set_gam(a, gam(a) + 2); break;
+            case P_CZ:  // M[a] ^= G[b]; M[b] ^= G[a]
+#pragma unroll
+                for (int w = 0; w < W; w++) {
+                    const uint64_t ga = tv.G[at(a, w)], gb = tv.G[at(b, w)];
+                    tv.M[at(a, w)] ^= gb;
+                    tv.M[at(b, w)] ^= ga;
+                }
+                break;
+            case P_CX: {  // c = a, t = b: γ_c += γ_t + 2·(M_c·F_t); F_c ^= F_t; M_c ^= M_t; G_t ^= G_c
+                int dot = 0;
+#pragma unroll
+                for (int w = 0; w < W; w++) dot += __popcll(tv.M[at(a, w)] & tv.F[at(b, w)]);
+                set_gam(a, gam(a) + gam(b) + 2 * (dot & 1));
+#pragma unroll
+                for (int w = 0; w < W; w++) {
+                    tv.F[at(a, w)] ^= tv.F[at(b, w)];
+                    tv.M[at(a, w)] ^= tv.M[at(b, w)];
+                    tv.G[at(b, w)] ^= tv.G[at(a, w)];
+                }
+                break;
+            }
+            case P_X:
+            case P_Y: {  // Y = i·X·Z: γ_a += 2 first, then the X rule, then the phase i
+                if (op == P_Y) set_gam(a, gam(a) + 2);
+                int beta = 0;
+#pragma unroll
+                for (int w = 0; w < W; w++) {
+                    const size_t o = (size_t)term * W + w;
+                    const uint64_t v = tv.V[o], s = tv.S[o], f = tv.F[at(a, w)], m = tv.M[at(a, w)];
+                    beta += __popcll((m & ~v & s) ^ (f & v & (m ^ s)));
+                    tv.S[o] = s ^ (f & ~v) ^ (m & v);
+                }
+                phase += 4 * (beta & 1) + 2 * gam(a) + (op == P_Y ? 2 : 0);
+                break;
+            }
+            default: break;  // the host sends no other op here
+        }
+    }
+    tv.phase[term] = (uint8_t)(phase & 7);
+}
+
 template <int W>
 __global__ void __launch_bounds__(WARPS * 32) project_kernel(TermsView tv, int q, int outcome,
                                                             int32_t* __restrict__ keep, int* __restrict__ status) {
@@ -696,6 +770,16 @@ cudaError_t launch_apply_ops(const uint32_t* d_ops, int nops, TermsView terms, i
         apply_ops_kernel<1><<<blocks_for(terms.chi), WARPS * 32, 0, st>>>(d_ops, nops, terms, status);
     else
         apply_ops_kernel<2><<<blocks_for(terms.chi), WARPS * 32, 0, st>>>(d_ops, nops, terms, status);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_ops(const RowOps& ops, TermsView terms, cudaStream_t st) {
+    if (terms.chi == 0 || ops.n == 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)((terms.chi + 255) / 256);
+    if (terms.W == 1)
+        row_ops_kernel<1><<<blocks, 256, 0, st>>>(terms, ops);
+    else
+        row_ops_kernel<2><<<blocks, 256, 0, st>>>(terms, ops);
     return cudaGetLastError();
 }
 

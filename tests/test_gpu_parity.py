@@ -287,6 +287,25 @@ def test_apply_gates_bit_exact(gpu_pkg, oracle, n, nc, nt, seed):
         st.apply_gates(np.asarray([[11, 0, 0, 0]], np.uint32))  # T on a compiled state
 
 
+@pytest.mark.parametrize("n,nt,seed", [(6, 8, 91), (40, 8, 92), (70, 6, 93)])
+def test_apply_gates_one_by_one_bit_exact(gpu_pkg, oracle, n, nt, seed):
+    """Gate-by-gate calls — a single gate without H, or a short list of them,
+    goes through the row kernel (one thread per term), lists with H through
+    the warp kernel — leave the terms of the whole list applied at once
+    (rows of one and two 64-bit words)."""
+    gates = random_full_circuit(n, 120, nt, seed)
+    extra = random_full_circuit(n, 90, 0, seed + 7)
+    st = gpu_pkg.QuantumState.from_gates(n, gates)
+    ref = oracle.OracleState.from_circuit(n, gates)
+    i = 0
+    while i < len(extra):
+        k = 3 if i % 4 == 0 else 1
+        st.apply_gates(extra[i:i + k])
+        i += k
+    ref.apply_gates(extra)
+    assert_same_terms(st.export_terms(), ref.export_terms())
+
+
 def test_error_codes(gpu_pkg):
     from stab_decomp_simulator_rust_gb300 import NecstarError
     QS, PS = gpu_pkg.QuantumState, gpu_pkg.PauliString
