@@ -300,7 +300,7 @@ def _gate_bytes(op, w):
 def gate_apply_leg(torch, stream, hbm_gbs):
     """Clifford application (nsg_apply_gates) on HBM-resident terms of the
     n = 60 and n = 64 workloads: 1,000 random {H,S,CX} gates fused in one
-    launch, and 48 of them gate by gate (one launch each)."""
+    launch, and 48 of them gate by gate (one call each), also split by kind."""
     from stab_decomp_simulator_rust_gb300 import QuantumState
     from stab_decomp_simulator_rust_gb300 import workloads as W
     out = {}
@@ -317,6 +317,12 @@ def gate_apply_leg(torch, stream, hbm_gbs):
         bytes_one = sum(_gate_bytes(g[0], n) for g in one) * chi
         ms_one, _ = _timed(torch, stream, lambda: [st.apply_gates(one[i:i + 1]) for i in range(len(one))], 2)
         term_bytes = 2 * (3 * 64 * 8 + 4 * 8 + 6)  # one read and one write of a whole term (n ≤ 64)
+        # by kind: H moves every term through a warp; S and CX (row kernel) touch their rows only
+        h_one = one[one[:, 0] == 0]
+        r_one = one[one[:, 0] != 0]
+        ms_h, _ = _timed(torch, stream, lambda: [st.apply_gates(h_one[i:i + 1]) for i in range(len(h_one))], 2)
+        ms_r, _ = _timed(torch, stream, lambda: [st.apply_gates(r_one[i:i + 1]) for i in range(len(r_one))], 2)
+        bytes_r = sum(_gate_bytes(g[0], n) for g in r_one) * chi
         out[name] = {
             "chi": chi, "state_bytes": int(chi * term_bytes // 2),
             "fused_1000_gates": {"ms": ms_fused, "algorithmic_GBps": bytes_run / (ms_fused * 1e-3) / 1e9,
@@ -325,12 +331,18 @@ def gate_apply_leg(torch, stream, hbm_gbs):
             "gate_by_gate": {"ms_per_gate": ms_one / len(one),
                              "algorithmic_GBps": bytes_one / (ms_one * 1e-3) / 1e9,
                              "frac_of_hbm": bytes_one / (ms_one * 1e-3) / 1e9 / hbm_gbs,
-                             "term_traffic_GBps": len(one) * chi * term_bytes / (ms_one * 1e-3) / 1e9,
-                             "term_traffic_frac_of_hbm": len(one) * chi * term_bytes / (ms_one * 1e-3) / 1e9 / hbm_gbs}}
+                             "h_gates": {"count": len(h_one), "ms_per_gate": ms_h / max(len(h_one), 1),
+                                         "term_traffic_GBps": len(h_one) * chi * term_bytes / (ms_h * 1e-3) / 1e9,
+                                         "term_traffic_frac_of_hbm":
+                                             len(h_one) * chi * term_bytes / (ms_h * 1e-3) / 1e9 / hbm_gbs},
+                             "s_cx_gates": {"count": len(r_one), "ms_per_gate": ms_r / max(len(r_one), 1),
+                                            "algorithmic_GBps": bytes_r / (ms_r * 1e-3) / 1e9,
+                                            "frac_of_hbm": bytes_r / (ms_r * 1e-3) / 1e9 / hbm_gbs}}}
         del st
     out["hbm_peak_GBps"] = hbm_gbs
-    out["note"] = ("algorithmic bytes per (gate, term): S 3*8W+2, CX 9*8W+3, H 5*8W+2*(3*w*8W); the kernel "
-                   "holds a whole term in registers, so one launch moves one term read+write whatever its gates")
+    out["note"] = ("algorithmic bytes per (gate, term): S 3*8W+2, CX 9*8W+3, H 5*8W+2*(3*w*8W); a launch with H "
+                   "holds whole terms in registers (one read and write of every term whatever its gates); a call "
+                   "with a single S or CX updates only the rows it touches (one thread per term)")
     return out
 
 
