@@ -514,6 +514,36 @@ __device__ __forceinline__ int fls0(Word x);  // index of the highest set bit
 template <>
 __device__ __forceinline__ int fls0<uint32_t>(uint32_t x) { return 31 - __clz(x); }
 
+// The alive variables coupled to no other alive variable, one ballot per row
+// slot.  They factor out together: an even L gives 2·δ(hb = 0) (IE), an odd
+// one √2·ω^{1-2hb} (IO).
+template <typename Word, int RPL>
+__device__ __forceinline__ Word isolated(const Word (&J)[RPL], Word alive, const Word (&own)[RPL]) {
+    Word iso = 0;
+#pragma unroll
+    for (int k = 0; k < RPL; k++)
+        iso |= (Word)__ballot_sync(FULL, own_bit<Word>(alive, k, (uint32_t)own[0]) && !(J[k] & alive & ~own[k]))
+               << (32 * k);
+    return iso;
+}
+
+// Variables e just joined IE: an observable whose high bit hb (hs ^ h) is set
+// on one of them has a zero term, whatever the rest of the sum (those bits
+// never change again).  True when every observable of the warp is zero
+// (zero[] is set on unused lanes), so the pair can stop: with many random
+// observables a pair often ends this way before its last rounds.
+template <typename Word, int NG>
+__device__ __forceinline__ bool all_zero_after(bool (&zero)[NG], Word hs, const Word (&h)[NG], Word e) {
+    if (!e) return false;  // nothing new (e is warp-uniform)
+    bool dead = true;
+#pragma unroll
+    for (int g = 0; g < NG; g++) {
+        zero[g] |= ((hs ^ h[g]) & e) != 0;
+        dead &= zero[g];
+    }
+    return __all_sync(FULL, dead);
+}
+
 // Sums out alive variables while one is left in `until` (the summation rounds
 // of the pair kernel).  A variable removed from `alive` keeps its bits of hs,
 // h and L0 from then on (every later update is masked by alive), so the
@@ -521,9 +551,11 @@ __device__ __forceinline__ int fls0<uint32_t>(uint32_t x) { return 31 - __clz(x)
 // summed-out variables with even L (a factor 2·δ(hb = 0)), IO those with odd L
 // (a factor √2·ω^{1-2hb}).  HIGH: pivots (and substituted variables) are the
 // highest candidates instead of the lowest.
+// Returns true when every observable's term became zero (the pair is done).
 template <typename Word, int RPL, int NG, bool HIGH>
-__device__ __forceinline__ void sum_out(Word (&J)[RPL], Word& hs, Word& L0, Word& alive, Word& IE, Word& IO, int& r,
-                                        Word (&h)[NG], int (&ph)[NG], const Word (&own)[RPL], const Word until) {
+__device__ __forceinline__ bool sum_out(Word (&J)[RPL], Word& hs, Word& L0, Word& alive, Word& IE, Word& IO, int& r,
+                                        Word (&h)[NG], int (&ph)[NG], bool (&zero)[NG], const Word (&own)[RPL],
+                                        const Word until) {
     while (alive & until) {
         // the next variable, with even L if there is one (an even step removes
         // two variables, which leaves fewer steps in all)
@@ -547,14 +579,11 @@ __device__ __forceinline__ void sum_out(Word (&J)[RPL], Word& hs, Word& L0, Word
             // variables factor out together, found by one ballot.  An elimination
             // never touches an isolated variable (its row and column are zero
             // among the alive ones), so they can wait until a pivot is one of them.
-            Word iso = 0;
-#pragma unroll
-            for (int k = 0; k < RPL; k++)
-                iso |= (Word)__ballot_sync(FULL, own_bit<Word>(alive, k, (uint32_t)own[0]) &&
-                                                     !(J[k] & alive & ~own[k])) << (32 * k);
+            const Word iso = isolated<Word, RPL>(J, alive, own);
             IE |= iso & ~L0;
             IO |= iso & L0;
             alive &= ~iso;
+            if (all_zero_after<Word, NG>(zero, hs, h, iso & ~L0)) return true;
             continue;
         }
         alive &= ~jb;
@@ -576,6 +605,7 @@ __device__ __forceinline__ void sum_out(Word (&J)[RPL], Word& hs, Word& L0, Word
             });
         }
     }
+    return false;
 }
 
 // MINB: blocks per SM the register allocation must allow (the register cap is
@@ -855,7 +885,7 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                     ph[g] = phB + 2 * gx + 4 * parity<Word>(((Mx ^ diag) & xf) ^ (xF & w));
                     h[g] = (x ^ Mx) & vA;
                     rhs[g] = (sB ^ xF) & cons;
-                    zero[g] = false;
+                    zero[g] = 32 * g + lane >= nobs;  // unused lanes count as zero
                 }
                 __syncwarp();  // sF/sJ are rewritten by the next ket
 
@@ -895,36 +925,45 @@ __global__ void __launch_bounds__(PWARPS * 32, MINB) pair_kernel(MultiLaunch p) 
                         g_subst<Word, RPL, NG, H>(q, lp, c, J, hs, L0, alive, h, ph, own);
                     });
                 }
-                // summation (sum_out)
+                // summation (sum_out); dead: every observable's term became zero
+                // on the way (sum_out stops there).
                 Word IE = 0, IO = 0;
+                bool dead;
                 if constexpr (sizeof(Word) == 8) {
                     // The variables of rows 32..63 first (highest first), then the
                     // rest on 32-bit words in one row slot: every update is masked by
                     // `alive`, so once no variable is left in the high half nothing
                     // above bit 31 changes again.
-                    sum_out<Word, RPL, NG, true>(J, hs, L0, alive, IE, IO, r, h, ph, own, ~(Word)0xffffffffu);
-                    uint32_t J32[1] = {(uint32_t)J[0]};
-                    const uint32_t own32[1] = {(uint32_t)own[0]};
-                    uint32_t hs32 = (uint32_t)hs, L032 = (uint32_t)L0, alive32 = (uint32_t)alive, IE32 = 0, IO32 = 0;
-                    uint32_t h32[NG];
+                    dead = sum_out<Word, RPL, NG, true>(J, hs, L0, alive, IE, IO, r, h, ph, zero, own,
+                                                        ~(Word)0xffffffffu);
+                    if (!dead) {
+                        uint32_t J32[1] = {(uint32_t)J[0]};
+                        const uint32_t own32[1] = {(uint32_t)own[0]};
+                        uint32_t hs32 = (uint32_t)hs, L032 = (uint32_t)L0, alive32 = (uint32_t)alive, IE32 = 0,
+                                 IO32 = 0;
+                        uint32_t h32[NG];
 #pragma unroll
-                    for (int g = 0; g < NG; g++) h32[g] = (uint32_t)h[g];
-                    sum_out<uint32_t, 1, NG, false>(J32, hs32, L032, alive32, IE32, IO32, r, h32, ph, own32, ~0u);
-                    const Word hi = ~(Word)0xffffffffu;
-                    hs = (hs & hi) | hs32;
+                        for (int g = 0; g < NG; g++) h32[g] = (uint32_t)h[g];
+                        dead = sum_out<uint32_t, 1, NG, false>(J32, hs32, L032, alive32, IE32, IO32, r, h32, ph, zero,
+                                                               own32, ~0u);
+                        const Word hi = ~(Word)0xffffffffu;
+                        hs = (hs & hi) | hs32;
 #pragma unroll
-                    for (int g = 0; g < NG; g++) h[g] = (h[g] & hi) | h32[g];
-                    IE |= IE32;
-                    IO |= IO32;
+                        for (int g = 0; g < NG; g++) h[g] = (h[g] & hi) | h32[g];
+                        IE |= IE32;
+                        IO |= IO32;
+                    }
                 } else {
-                    sum_out<Word, RPL, NG, false>(J, hs, L0, alive, IE, IO, r, h, ph, own, ~(Word)0);
+                    dead = sum_out<Word, RPL, NG, false>(J, hs, L0, alive, IE, IO, r, h, ph, zero, own, ~(Word)0);
                 }
-                r -= 2 * popc<Word>(IE) + popc<Word>(IO);
+                if (!dead) {
+                    r -= 2 * popc<Word>(IE) + popc<Word>(IO);
 #pragma unroll
-                for (int g = 0; g < NG; g++) {
-                    const Word hbits = hs ^ h[g];
-                    zero[g] |= (hbits & IE) != 0;
-                    ph[g] += popc<Word>(IO) - 2 * popc<Word>(hbits & IO);
+                    for (int g = 0; g < NG; g++) {
+                        const Word hbits = hs ^ h[g];
+                        zero[g] |= (hbits & IE) != 0;
+                        ph[g] += popc<Word>(IO) - 2 * popc<Word>(hbits & IO);
+                    }
                 }
 
                 const int kpair = (kcB - kcA) & 7;
