@@ -64,9 +64,11 @@ WORKLOAD = "512 circuits, n~U[8,64], t~U[4,32], 20n {H,S,CX}, 16 dense Paulis ea
 
 # DRAM bytes (read + write) of the 64-bit-row pair launch of one step of the
 # default workload, with the tiling its plan tunes (16 kets per chunk, 256
-# tasks per resident warp), from one ncu capture of this build:
+# tasks per resident warp), from one ncu capture of that launch:
 # dram__bytes_read.sum 3.31 GB + dram__bytes_write.sum 0.48 GB (the ket
-# tables ≈ 2 GB read about once, task records, frames).
+# tables ≈ 2 GB read about once, task records, frames).  The kernel's later
+# arithmetic changes left its reads unchanged (296 MB on a 20-state capture
+# before and after them).
 PAIR_TRAFFIC_BYTES = 3_310_000_000 + 483_440_000
 
 
