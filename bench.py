@@ -19,6 +19,9 @@ step over Σχ(χ+1)/2 ≈ 1.04·10⁹ term pairs.
 * ``exactness``: every one of the 8,192 results of the timed path (and of
   the FP64 batched path) against the exact sum of its pair terms
   (nsg_exp_value_counts: integer counts per power of √2, evaluated exactly).
+* ``zero_screen``: the common-stabilizer test (nsg_zero_screen, host work,
+  not used by ``value``): how many of the exactly-zero observables it decides
+  without pair work, and how many it decides that are not zero (must be 0).
 * ``e2e``: the same metric end to end through the C ABI from host buffers:
   nsg_states_from_circuits (512 gate lists from pinned host memory) +
   nsg_exp_value_multi (Paulis from host, 8,192 doubles back), wall clock.
@@ -449,6 +452,16 @@ def run_ours(args):
                  "fp64_batched_vs_exact": _exact_errors(flat(v64), flat(exact)),
                  "exact_path": "nsg_exp_value_counts per circuit (signed counts per power of sqrt 2), summed exactly",
                  "exact_s": exact_s}
+    # ---- the common-stabilizer zero test (host only, not used by the timed path): how many of the
+    # exactly-zero observables it decides without pair work, and that every one it decides is zero
+    t0 = time.perf_counter()
+    screened = np.concatenate([s.zero_screen(ps) for s, ps in zip(states, plists)])
+    screen_s = time.perf_counter() - t0
+    ex_flat = flat(exact)
+    zero_screen = {"decided_zero": int(screened.sum()), "exact_zero": int((ex_flat == 0.0).sum()),
+                   "decided_but_nonzero": int((screened & (ex_flat != 0.0)).sum()), "observables": int(len(ex_flat)),
+                   "host_s": screen_s,
+                   "note": "nsg_zero_screen: P anticommutes with a stabilizer common to every term; not used by value"}
 
     # ---- plain: one circuit and one observable per call, FP64 (4 of the 16 observables of every circuit)
     per = max(1, min(args.plain_observables, 16))
@@ -515,7 +528,7 @@ def run_ours(args):
                               f"({per} of the 16 observables of each of the 512 circuits)",
                       "vs_exact": plain_err},
             "speedup_vs_plain": value / plain_value,
-            "exactness": exactness, "e2e": e2e, "roofline": roofline, "gate_apply": gates_leg,
+            "exactness": exactness, "zero_screen": zero_screen, "e2e": e2e, "roofline": roofline, "gate_apply": gates_leg,
             "plain40": p40, "clocks": clocks.summary(),
             # per replay: frames and term tables per state, Pauli frames per state, and per row
             # width (32- and 64-bit) one pair launch and two reduction passes

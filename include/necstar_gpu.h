@@ -228,6 +228,23 @@ nsg_status nsg_exp_value_multi(const nsg_state* const* states, size_t num_states
 nsg_status nsg_exp_value_counts(const nsg_state* state, const nsg_pauli* paulis, size_t num_paulis,
                                 int64_t* counts, double* scale);
 
+/* Observables whose ⟨P⟩ is exactly 0 without any pair work (no reference
+ * counterpart; exp_value itself always sums the pairs).  A compiled state is
+ * (1 ⊗ ⟨0|^t) U' (|0^n⟩ ⊗ |T⟩^{⊗t}) with U' the lowered circuit (T and Tdg as a
+ * CX onto an ancilla); the images under U' of data-qubit Z strings with no X
+ * component on the ancillas are, restricted to the data qubits, stabilizers
+ * common to every term, and a Pauli that anticommutes with one of them has a
+ * zero term for every pair.  zero[i] = 1: ⟨P_i⟩ = 0 exactly; 0: not decided by
+ * this test.  The generators follow Clifford gates (nsg_apply_gates), clones
+ * and term selections; projection, discard and measurement drop them (every
+ * entry 0 afterwards), as do states not made by compiling a circuit.  Host
+ * work only, O(n) words per observable. */
+nsg_status nsg_zero_screen(const nsg_state* state, const nsg_pauli* paulis, size_t num_paulis, uint8_t* zero);
+/* The same test for a circuit, without compiling it (host only; no GPU
+ * needed); the circuit's checks and errors are nsg_state_from_circuit's. */
+nsg_status nsg_zero_screen_circuit(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates,
+                                   const nsg_pauli* paulis, size_t num_paulis, uint8_t* zero);
+
 /* Tiling of the direct (uncaptured) pair sums of this process: kets per
  * chunk and tasks per resident warp of the persistent pair launch; 0 takes
  * the tuned choice of the workload class if a plan tuned one, else the

@@ -8,8 +8,8 @@ include/necstar_gpu.h).
 """
 from .circuit import QuantumCircuit, QuantumGate
 from .pauli import PauliString
-from .state import PRECISION_FP64, PRECISION_MIXED, BatchPlan, QuantumState, exp_values_multi
+from .state import PRECISION_FP64, PRECISION_MIXED, BatchPlan, QuantumState, exp_values_multi, zero_screen_circuit
 from ._ffi import NecstarError
 
 __all__ = ["QuantumCircuit", "QuantumGate", "PauliString", "QuantumState", "NecstarError",
-           "PRECISION_FP64", "PRECISION_MIXED", "exp_values_multi", "BatchPlan"]
+           "PRECISION_FP64", "PRECISION_MIXED", "exp_values_multi", "BatchPlan", "zero_screen_circuit"]

@@ -91,6 +91,8 @@ def load(path: str | None = None):
     L.nsg_profile_read.argtypes = [P(dbl), P(u64), P(u64)]
     L.nsg_probe_int_ops.argtypes = [u64, P(dbl), P(u64)]
     L.nsg_exp_value_counts.argtypes = [vp, P(PauliABI), sz, vp, P(dbl)]
+    L.nsg_zero_screen.argtypes = [vp, P(PauliABI), sz, vp]
+    L.nsg_zero_screen_circuit.argtypes = [u32, vp, sz, P(PauliABI), sz, vp]
     L.nsg_set_pair_tiling.argtypes = [i32, i32]
     L.nsg_debug_compile_keep.argtypes = [u32, vp, sz, vp, sz, P(u64)]
     L.nsg_state_select.argtypes = [vp, vp, sz, P(vp)]

@@ -434,6 +434,78 @@ static bool state_alive(const nsg_state* s, uint64_t uid) {
     return it != g_states.end() && it->second == uid;
 }
 
+// Stabilizers common to every term of a compiled state (the zero test of
+// nsg_zero_screen).  The state is (1 ⊗ ⟨0|^t) U' (|0^n⟩ ⊗ |T⟩^{⊗t}) with U'
+// the lowered circuit (T, Tdg = CX onto an ancilla [+ Sdg]); for a data
+// Z string Z^a, R = U' (Z^a ⊗ 1) U'† satisfies R·U'(|0^n⟩ ⊗ φ) = U'(|0^n⟩ ⊗ φ)
+// for every ancilla state φ, and when R has no X component on the ancillas
+// (1 ⊗ ⟨0|^t) R = ±R_d (1 ⊗ ⟨0|^t), so ±R_d stabilizes every term.  A Pauli P
+// that anticommutes with such an R_d has ⟨s_a|P|s_b⟩ = 0 for every pair, so
+// ⟨P⟩ = 0 exactly.  Bit-sliced images (signs are not needed): bit j of
+// sx[q] / sz[q] is the x / z bit at qubit q of the image of Z_j; the ancilla
+// X parts span `anc` (an XOR basis, one vector per leading bit).  P = X(px)
+// Z(pz) anticommutes with the image of Z^a iff a·v_P = 1, v_P = ⊕_{q ∈ px} sz[q]
+// ⊕ ⊕_{q ∈ pz} sx[q]; such an a with no ancilla X part exists iff v_P is
+// outside the span of the ancilla rows.
+struct ZeroScreen {
+    int n = 0;
+    uint64_t sx[64] = {}, sz[64] = {};
+    uint64_t anc[64] = {};  // anc[b]: the basis vector whose highest bit is b (0 = none)
+
+    // Conjugation of every image by one primitive op (gates act on qubits < w).
+    static void conj(uint64_t* X, uint64_t* Z, uint32_t code) {
+        const uint32_t op = code & 0xff, a = (code >> 8) & 0xff, b = (code >> 16) & 0xff;
+        switch (op) {
+            case P_H: std::swap(X[a], Z[a]); break;
+            case P_S:
+            case P_SDG: Z[a] ^= X[a]; break;
+            case P_CX: X[b] ^= X[a]; Z[a] ^= Z[b]; break;  // control a, target b
+            case P_CZ: Z[a] ^= X[b]; Z[b] ^= X[a]; break;
+            default: break;  // X, Y, Z change signs only
+        }
+    }
+    void insert_anc(uint64_t v) {
+        for (int bit = 63; bit >= 0 && v; bit--) {
+            if (!((v >> bit) & 1)) continue;
+            if (!anc[bit]) {
+                anc[bit] = v;
+                return;
+            }
+            v ^= anc[bit];
+        }
+    }
+    bool zero(uint64_t px, uint64_t pz) const {
+        uint64_t v = 0;
+        for (int q = 0; q < n; q++) {
+            if ((px >> q) & 1) v ^= sz[q];
+            if ((pz >> q) & 1) v ^= sx[q];
+        }
+        for (int bit = 63; bit >= 0 && v; bit--)
+            if (((v >> bit) & 1) && anc[bit]) v ^= anc[bit];
+        return v != 0;
+    }
+    void apply(const std::vector<uint32_t>& ops) {  // Clifford gates on the n data qubits
+        for (uint32_t c : ops) conj(sx, sz, c);
+    }
+};
+
+// The zero test of a lowered circuit (n ≤ 64; null beyond).
+std::shared_ptr<const ZeroScreen> screen_of(int n, int t, const std::vector<uint32_t>& ops) {
+    if (n > 64) return nullptr;
+    const int w = n + t;
+    std::vector<uint64_t> X((size_t)w, 0), Z((size_t)w, 0);
+    for (int j = 0; j < n; j++) Z[j] = 1ull << j;
+    for (uint32_t c : ops) ZeroScreen::conj(X.data(), Z.data(), c);
+    auto s = std::make_shared<ZeroScreen>();
+    s->n = n;
+    for (int q = 0; q < n; q++) {
+        s->sx[q] = X[q];
+        s->sz[q] = Z[q];
+    }
+    for (int q = n; q < w; q++) s->insert_anc(X[q]);
+    return s;
+}
+
 struct nsg_state {
     int device = 0;
     cudaStream_t own = nullptr;
@@ -442,6 +514,9 @@ struct nsg_state {
     double gf_re = 1.0, gf_im = 0.0;
     uint64_t uid = 0;         // process-unique identity (plans check it)
     uint64_t layout_gen = 0;  // bumped whenever the term storage is replaced or reshaped
+    // Common stabilizers of the terms (compiled states, through Clifford
+    // gates); null when unknown.  Shared between clones, replaced on change.
+    std::shared_ptr<const ZeroScreen> screen;
     // cached bra frames
     bool frames_ok = false;
     DBuf<uint64_t> fGV, fFV, fMV, fGVL, fGVH;
@@ -591,6 +666,7 @@ void compact_into(nsg_state* s, DBuf<int32_t>& keep) {
     s->t = std::move(out);
     s->layout_gen++;
     s->invalidate();
+    s->screen.reset();  // a projection: the common stabilizers are no longer known
 }
 
 // Process-wide pair-kernel timing (nsg_profile_*).
@@ -1205,6 +1281,15 @@ void discard_q(nsg_state* s, uint32_t q) {  // discard.rs:5-12
     s->t.n -= 1;
     s->layout_gen++;
     s->invalidate();
+    s->screen.reset();
+}
+
+// Clifford gates applied to a state move its common stabilizers with them.
+void conj_screen(nsg_state* s, const std::vector<uint32_t>& ops) {
+    if (!s->screen) return;
+    auto ns = std::make_shared<ZeroScreen>(*s->screen);
+    ns->apply(ops);
+    s->screen = std::move(ns);
 }
 
 void apply_ops(nsg_state* s, const std::vector<uint32_t>& ops) {
@@ -1220,6 +1305,7 @@ void apply_ops(nsg_state* s, const std::vector<uint32_t>& ops) {
         for (size_t i = 0; i < ops.size(); i++) r.code[i] = ops[i];
         CK(launch_row_ops(r, s->t.view(), s->st));
         s->invalidate();
+        conj_screen(s, ops);
         return;
     }
     DBuf<uint32_t> d;
@@ -1228,6 +1314,7 @@ void apply_ops(nsg_state* s, const std::vector<uint32_t>& ops) {
     CK(launch_apply_ops(d.p, (int)ops.size(), s->t.view(), s->status.p, s->st));
     s->check_status();
     s->invalidate();
+    conj_screen(s, ops);
 }
 
 nsg_state* clone_state(const nsg_state* s) {
@@ -1237,6 +1324,7 @@ nsg_state* clone_state(const nsg_state* s) {
     c->t.copy_from(s->t, c->st);
     c->gf_re = s->gf_re;
     c->gf_im = s->gf_im;
+    c->screen = s->screen;
     CK(cudaStreamSynchronize(c->st));
     return c;
 }
@@ -1596,6 +1684,7 @@ std::unique_ptr<nsg_state> compile_state(uint32_t num_qubits, const nsg_gate* ga
     const Lowered lw = lower_circuit(num_qubits, gates, num_gates);
     compile_enqueue(lw, lw.ops.data(), pc);
     compile_finish(pc, keep_out);
+    pc.s->screen = screen_of(lw.n, lw.t, lw.ops);
     return std::move(pc.s);
 }
 }  // namespace
@@ -1667,6 +1756,7 @@ nsg_status nsg_states_from_circuits(size_t num_circuits, const uint32_t* num_qub
     for (size_t c = 0; c < num_circuits; c++) {
         try {
             compile_finish(pend[c], nullptr);
+            pend[c].s->screen = screen_of(lw[c].n, lw[c].t, lw[c].ops);
         } catch (const ApiError& e) {
             g_args[2] = (int64_t)c;
             sync_all();
@@ -1714,6 +1804,7 @@ nsg_status nsg_state_select(const nsg_state* cstate, const uint64_t* indices, si
     keep.alloc(hk.size(), s->st);
     CK(cudaMemcpyAsync(keep.p, hk.data(), hk.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
     compact_into(s.get(), keep);
+    s->screen = cstate->screen;  // every kept term keeps the common stabilizers
     *out = s.release();
     API_END
 }
@@ -1861,6 +1952,40 @@ nsg_status nsg_apply_gates(nsg_state* state, const nsg_gate* gates, size_t num_g
 
 nsg_status nsg_exp_value(const nsg_state* state, const nsg_pauli* pauli, double* out) {
     return nsg_exp_value_batch(state, pauli, 1, NSG_PRECISION_FP64, out);
+}
+
+nsg_status nsg_zero_screen(const nsg_state* cstate, const nsg_pauli* paulis, size_t num_paulis, uint8_t* zero) {
+    API_BEGIN
+    need(cstate, "state");
+    if (num_paulis) {
+        need(paulis, "paulis");
+        need(zero, "zero");
+    }
+    nsg_state* state = const_cast<nsg_state*>(cstate);
+    require_pairs_width(state);
+    const std::shared_ptr<const ZeroScreen> sc = state->screen;
+    for (size_t i = 0; i < num_paulis; i++) {
+        const DevPauli d = to_dev_pauli(paulis[i], state->t.n);
+        zero[i] = (sc && sc->zero(d.px, d.pz)) ? 1 : 0;
+    }
+    API_END
+}
+
+nsg_status nsg_zero_screen_circuit(uint32_t num_qubits, const nsg_gate* gates, size_t num_gates,
+                                   const nsg_pauli* paulis, size_t num_paulis, uint8_t* zero) {
+    API_BEGIN
+    if (num_paulis) {
+        need(paulis, "paulis");
+        need(zero, "zero");
+    }
+    const Lowered lw = lower_circuit(num_qubits, gates, num_gates);
+    if (lw.n > 64) raise(NSG_ERR_TOO_WIDE, lw.n, 64, "state width %d exceeds the supported 64 qubits", lw.n);
+    const std::shared_ptr<const ZeroScreen> sc = screen_of(lw.n, lw.t, lw.ops);
+    for (size_t i = 0; i < num_paulis; i++) {
+        const DevPauli d = to_dev_pauli(paulis[i], lw.n);
+        zero[i] = sc->zero(d.px, d.pz) ? 1 : 0;
+    }
+    API_END
 }
 
 nsg_status nsg_exp_value_batch(const nsg_state* cstate, const nsg_pauli* paulis, size_t num_paulis,

@@ -80,6 +80,26 @@ def _p(a: np.ndarray | None):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
 
 
+def _pauli_array(paulis):
+    """The ABI array of a list of PauliString (and the list, which keeps their buffers alive)."""
+    paulis = list(paulis)
+    arr = (_ffi.PauliABI * max(len(paulis), 1))()
+    for i, p in enumerate(paulis):
+        arr[i] = p.abi()
+    return arr, paulis
+
+
+def zero_screen_circuit(num_qubits: int, gates, paulis) -> np.ndarray:
+    """The common-stabilizer zero test for a circuit, without compiling it
+    (nsg_zero_screen_circuit; host work only): True where ⟨P⟩ = 0 exactly on the
+    circuit's compiled state, False where the test does not decide."""
+    rows = gate_rows(gates)
+    arr, keep = _pauli_array(paulis)
+    out = np.zeros(len(keep), np.uint8)
+    check(_ffi.load().nsg_zero_screen_circuit(num_qubits, _p(rows), len(rows), arr, len(keep), _p(out)))
+    return out.astype(bool)
+
+
 class QuantumState:
     def __init__(self, handle: C.c_void_p):
         self._h = handle
@@ -211,6 +231,15 @@ class QuantumState:
         scale = C.c_double()
         check(_ffi.load().nsg_exp_value_counts(self._h, arr, len(paulis), _p(counts), C.byref(scale)))
         return counts, scale.value
+
+    def zero_screen(self, paulis) -> np.ndarray:
+        """Observables with ⟨P⟩ = 0 exactly by the common-stabilizer test
+        (nsg_zero_screen): True = provably zero, False = not decided.  No pair
+        work; exp_value does not use it."""
+        arr, keep = _pauli_array(paulis)
+        out = np.zeros(len(keep), np.uint8)
+        check(_ffi.load().nsg_zero_screen(self._h, arr, len(keep), _p(out)))
+        return out.astype(bool)
 
     def exp_values_exact(self, paulis) -> np.ndarray:
         """⟨P⟩ rounded once from the exact sum of every pair term."""

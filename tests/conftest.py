@@ -60,6 +60,17 @@ def oracle():
 
 
 @pytest.fixture(scope="session")
+def host_pkg():
+    """The product package with its library loaded, for entry points that do
+    host work only (no GPU call)."""
+    from stab_decomp_simulator_rust_gb300 import _ffi, build
+    build.build()
+    _ffi.load()
+    import stab_decomp_simulator_rust_gb300 as pkg
+    return pkg
+
+
+@pytest.fixture(scope="session")
 def gpu_pkg():
     """The product package with its CUDA library loaded (built if missing)."""
     from stab_decomp_simulator_rust_gb300 import _ffi, build
