@@ -472,10 +472,10 @@ def run_ours(args):
     rest = [i for i, z in enumerate(per_state) if not z.all()]
     screened_line = None
     if rest:
-        plan_s = BatchPlan([states[i] for i in rest], [plists[i] for i in rest], PRECISION_MIXED)
-        vs = plan_s.run()
-        ms_s, _ = _timed(torch, stream, plan_s.run, max(1, min(3, args.steps)))
-        del plan_s
+        splan = BatchPlan([states[i] for i in rest], [plists[i] for i in rest], PRECISION_MIXED)
+        vs = splan.run()
+        ms_s, _ = _timed(torch, stream, splan.run, max(1, min(3, args.steps)))
+        del splan
         got = [np.zeros(len(ps)) for ps in plists]
         for k, i in enumerate(rest):
             got[i] = np.asarray(vs[k], float)
