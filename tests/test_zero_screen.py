@@ -72,3 +72,33 @@ def test_screen_errors(host_pkg):
     with pytest.raises(NecstarError) as e:
         pkg.zero_screen_circuit(70, np.zeros((0, 4), np.uint32), [])
     assert e.value.code == codes["NSG_ERR_TOO_WIDE"]
+
+
+def test_screen_dense_and_sparse_agree(host_pkg):
+    """A Pauli given sparse (qubits and ops) is screened like the same Pauli given dense."""
+    pkg = host_pkg
+    n = 12
+    g = random_full_circuit(n, 150, 5, 311)
+    rng = np.random.default_rng(311)
+    dense, sparse = [], []
+    for _ in range(40):
+        ops = rng.integers(0, 4, n).astype(np.uint8)
+        dense.append(pkg.PauliString.dense(ops))
+        q = np.flatnonzero(ops).astype(np.uint32)
+        sparse.append(pkg.PauliString.sparse(ops[q], q))
+    np.testing.assert_array_equal(pkg.zero_screen_circuit(n, g, dense), pkg.zero_screen_circuit(n, g, sparse))
+
+
+def test_screen_without_t_gates_is_the_stabilizer_group(host_pkg, oracle):
+    """With no T gate the state is one stabilizer state: P is decided zero
+    exactly when it is not ± an element of its stabilizer group."""
+    pkg = host_pkg
+    n = 5
+    g = random_full_circuit(n, 60, 0, 312)
+    ref = oracle.OracleState.from_circuit(n, g)
+    every = [pkg.PauliString.dense(np.array([(k >> (2 * q)) & 3 for q in range(n)], np.uint8))
+             for k in range(4 ** n)]
+    z = pkg.zero_screen_circuit(n, g, every)
+    for p, zz in zip(every, z):
+        v = ref.exp_value(0, p.ops)[1]
+        assert zz == (v == 0.0), (p, v)
