@@ -207,11 +207,15 @@ __device__ __forceinline__ void apply_prim(Eng<W, RPL, Word>& e, uint32_t code) 
     uint32_t op = code & 0xff, a = (code >> 8) & 0xff, b = (code >> 16) & 0xff;
     switch (op) {
         case P_H: e.left_h(a); break;
-        case P_X: e.left_x(a); break;
-        case P_Y: e.left_y(a); break;
+        case P_X:
+        case P_Y:  // one copy of the X rule: Y = i·X·Z
+            if (op == P_Y) e.left_z(a);
+            e.left_x(a);
+            if (op == P_Y) e.phase = (e.phase + 2) & 7;
+            break;
         case P_Z: e.left_z(a); break;
-        case P_S: e.left_s(a); break;
-        case P_SDG: e.left_sdg(a); break;
+        case P_S:
+        case P_SDG: e.left_s_like(a, op == P_S ? 3 : 1); break;  // one copy of the S rule
         case P_CX: e.left_cx(a, b); break;
         case P_CZ: e.left_cz(a, b); break;
         default: e.err = 9; break;
