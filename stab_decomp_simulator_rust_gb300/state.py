@@ -209,9 +209,13 @@ class QuantumState:
         check(_ffi.load().nsg_exp_value(self._h, C.byref(a), C.byref(out)))
         return out.value
 
-    def exp_values(self, paulis, precision: int = PRECISION_FP64) -> np.ndarray:
-        """Batched expectation values: one pass over the pairs for all observables."""
+    def exp_values(self, paulis, precision: int = PRECISION_FP64, screen: bool = False) -> np.ndarray:
+        """Batched expectation values: one pass over the pairs for all observables.
+        screen=True (opt-in): when the common-stabilizer test (zero_screen)
+        decides every observable, return the exact zeros without the pair pass."""
         paulis = list(paulis)
+        if screen and paulis and self.zero_screen(paulis).all():
+            return np.zeros(len(paulis), np.float64)
         arr = (_ffi.PauliABI * max(len(paulis), 1))()
         for i, p in enumerate(paulis):
             arr[i] = p.abi()
@@ -452,11 +456,25 @@ class BatchPlan:
         return out
 
 
-def exp_values_multi(states, paulis_per_state, precision: int = PRECISION_FP64) -> list[np.ndarray]:
+def exp_values_multi(states, paulis_per_state, precision: int = PRECISION_FP64,
+                     screen: bool = False) -> list[np.ndarray]:
     """⟨P⟩ for many states at once: observables ``paulis_per_state[c]`` on
     ``states[c]``, every pair sum in one persistent launch (one per row width:
     ≤ 32 and > 32 qubits).  Returns one array per state, each value as
-    ``states[c].exp_values(paulis_per_state[c], precision)`` gives it."""
+    ``states[c].exp_values(paulis_per_state[c], precision)`` gives it.
+    screen=True (opt-in): states whose every observable the common-stabilizer
+    test (QuantumState.zero_screen) decides get the exact zeros without a pair
+    sum; the others are summed as usual."""
+    if screen:
+        states, paulis_per_state = list(states), [list(p) for p in paulis_per_state]
+        done = [bool(ps) and s.zero_screen(ps).all() for s, ps in zip(states, paulis_per_state)]
+        rest = [c for c in range(len(states)) if not done[c]]
+        out = [np.zeros(len(ps), np.float64) for ps in paulis_per_state]
+        if rest:
+            got = exp_values_multi([states[c] for c in rest], [paulis_per_state[c] for c in rest], precision)
+            for k, c in enumerate(rest):
+                out[c] = got[k]
+        return out
     states, groups, offs, total, arr, hs = _multi_args(states, paulis_per_state)
     out = np.zeros(max(total, 1), np.float64)
     check(_ffi.load().nsg_exp_value_multi(hs, len(states), arr, _p(offs), precision, _p(out)))
